@@ -1,0 +1,435 @@
+"""Benchmark: line integral convolution throughput on GB300.
+
+Workload (one "step"): rlic.convolve on the at-scale case, 8192 x 8192
+float32, 65-tap Hann kernel, polarization mode, boundaries
+{x: periodic, y: closed}, 5 iterations (rlic_gb300.workloads.
+fourier_vortex_case).  Metric: Gsamples/s = H * W * K * iterations / time.
+
+  value     device-resident inputs, rlic_convolve_f32 on device pointers
+            (pack + 5 passes per step), CUDA events on the launching stream;
+  e2e       the public API rlic_gb300.convolve on host (pinned) numpy
+            arrays: validation, host->device copies, compute, device->host
+            copy of the result, all inside the timed region;
+  roofline  the dominant kernel (one convolution pass) timed per launch:
+            algorithmic bytes s*(3K-1) per pixel per pass over its duration,
+            against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (a restatement of the reference's Rust
+            core) timed on a bounded band of rows of the same workload.
+
+--impl reference times the CPU restatement of the reference's
+implementation on all host threads (the reference's Rust core cannot be
+built here), with the same metric and config.
+
+Multi-GPU (torchrun, one rank per GPU): every rank convolves its own full
+instance (the image does not need to be split to fill a GPU), so the work
+per GPU is fixed and value = total samples / max time over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+if str(REPO) not in sys.path:
+    sys.path.insert(0, str(REPO))
+
+N_DEFAULT = 8192
+KLEN = 65
+ITERS = 5
+METRIC = "Gsamples/s (px x kernel x iters)"
+UNIT = "Gsamples/s"
+
+
+def parse_args() -> argparse.Namespace:
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--size", type=int, default=N_DEFAULT, help="image side (default 8192)")
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="target CPU time of the oracle baseline sample")
+    p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def config(n: int) -> dict:
+    return {
+        "workload": f"fourier_vortex_{n}x{n}_f32_hann{KLEN}_polarization_xperiodic_yclosed_n{ITERS}",
+        "size": [n, n],
+        "klen": KLEN,
+        "kernel": "hann",
+        "uv_mode": "polarization",
+        "boundaries": {"x": "periodic", "y": "closed"},
+        "iterations": ITERS,
+        "form": "plain (one thread per pixel, packed (u,v), L1-cached gathers)",
+        "l2": "inputs larger than L2 (texture 256 MiB, packed field 512 MiB at 8192^2)",
+    }
+
+
+# ------------------------------------------------------------ distributed --
+
+class Dist:
+    def __init__(self) -> None:
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+
+    def init(self, backend: str) -> None:
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self) -> None:
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, x: float, device) -> float:
+        if self.pg is None:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    """nvidia-smi samples every 100 ms while the timed region runs."""
+
+    FIELDS = ("pci.bus_id,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, pci: tuple[int, int, int] | None) -> None:
+        self.pci = pci
+        self.proc = None
+        fd, name = tempfile.mkstemp(prefix="rlic_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc) -> None:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    @staticmethod
+    def _pci(text: str) -> tuple[int, int, int] | None:
+        try:
+            dom, bus, rest = text.strip().split(":")
+            return int(dom, 16), int(bus, 16), int(rest.split(".")[0], 16)
+        except ValueError:
+            return None
+
+    def summary(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [[x.strip() for x in line.split(",")]
+                for line in self.path.read_text().splitlines()]
+        self.path.unlink(missing_ok=True)
+        rows = [r for r in rows if len(r) == 8]
+        if self.pci is not None and any(self._pci(r[0]) == self.pci for r in rows):
+            rows = [r for r in rows if self._pci(r[0]) == self.pci]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x: str) -> float | None:
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = sorted({self.REASONS[i] for r in rows for i in range(4) if r[4 + i] == "Active"})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": reasons,
+            "samples": len(rows),
+        }
+
+
+# -------------------------------------------------------------- CPU legs --
+
+def cpu_sample(case_np: dict, seconds: float, threads: int) -> dict:
+    """Times the oracle on a band of rows of one pass, sized to ~`seconds`."""
+    from oracle import oracle
+
+    tex, u, v, k = (case_np[x] for x in ("texture", "u", "v", "kernel"))
+    ny, nx = tex.shape
+    kw = dict(uv_mode=case_np["uv_mode"], boundaries=case_np["boundaries"], nthreads=threads)
+    rows = max(threads, 8)
+    r0 = ny // 2
+    t0 = time.perf_counter()
+    oracle.sweep_rows(tex, u, v, k, r0, min(ny, r0 + rows), **kw)
+    dt = time.perf_counter() - t0
+    rows = int(min(ny, max(rows, rows * seconds / max(dt, 1e-6))))
+    r0 = max(0, ny // 2 - rows // 2)
+    t0 = time.perf_counter()
+    oracle.sweep_rows(tex, u, v, k, r0, r0 + rows, **kw)
+    dt = time.perf_counter() - t0
+    samples = rows * nx * k.size
+    return {
+        "value": samples / dt / 1e9,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"rows [{r0}, {r0 + rows}) of one pass over the {ny}x{nx} workload "
+                  f"({samples:.3e} samples, {dt:.2f} s) with the C oracle, {threads} threads",
+        "seconds": dt,
+    }
+
+
+def run_reference(args, dist: Dist) -> None:
+    """The CPU restatement of the reference's implementation, timed on the host."""
+    if dist.rank != 0:
+        return
+    from oracle import oracle
+    from rlic_gb300.workloads import fourier_vortex_case
+
+    threads = oracle.env_threads()
+    case = fourier_vortex_case(n=args.size, device="cpu")
+    per_step = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_sample(case, min(per_step, 3.0), threads)
+    vals, times = [], []
+    for _ in range(args.steps):
+        r = cpu_sample(case, per_step, threads)
+        vals.append(r["value"])
+        times.append(r["seconds"])
+    value = float(statistics.median(vals))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(statistics.median(times)),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded Fourier modes + point vortices, 1% zero cells)",
+        "config": config(args.size),
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": r["sample"] + "; the reference's Rust core cannot be built here "
+                      "(no Rust toolchain), so its C restatement is timed",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU leg --
+
+def run_gb300(args, dist: Dist) -> None:
+    import torch
+
+    import rlic_gb300
+    from rlic_gb300 import _native
+    from rlic_gb300.workloads import fourier_vortex_case
+
+    dist.init("nccl")
+    dev = torch.device("cuda", dist.local_rank)
+    torch.cuda.set_device(dev)
+    lib = _native.lib()
+    n = args.size
+    case = fourier_vortex_case(n=n, device=str(dev), as_numpy=False)
+    tex, u, v, k = (case[x].contiguous() for x in ("texture", "u", "v", "kernel"))
+    bcodes = (1, 1, 0, 0)
+    uv_code = 1
+    samples = n * n * KLEN * ITERS
+    out = torch.empty_like(tex)
+    nbytes = lib.rlic_workspace_bytes(n, n, KLEN, ITERS, 4)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step() -> None:
+        _native.check(lib.rlic_convolve_f32(
+            tex.data_ptr(), u.data_ptr(), v.data_ptr(), n, n, k.data_ptr(), KLEN, uv_code,
+            *bcodes, ITERS, out.data_ptr(), ws.data_ptr(), nbytes, sp, 0))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    props = torch.cuda.get_device_properties(dev)
+    pci = None
+    if all(hasattr(props, a) for a in ("pci_domain_id", "pci_bus_id", "pci_device_id")):
+        pci = (props.pci_domain_id, props.pci_bus_id, props.pci_device_id)
+
+    launches0 = _native.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(pci) as clocks:
+        dist.barrier()
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        dist.barrier()
+    launches = _native.launch_count() - launches0
+    ms_local = ev0.elapsed_time(ev1)
+    ms_total = dist.max(ms_local, dev)
+    ms_step = ms_total / args.steps
+    value = dist.world * samples * args.steps / (ms_total / 1e3) / 1e9
+
+    # ---- dominant kernel: one pass, timed per launch on the same stream
+    uv = torch.empty((n, n, 2), dtype=torch.float32, device=dev)
+    _native.check(lib.rlic_pack_field_f32(u.data_ptr(), v.data_ptr(), n, n, uv.data_ptr(), sp))
+    tmp = torch.empty_like(tex)
+    passes = max(6, args.steps)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(passes + 2)]
+    for a, b in evs:  # same pure pass each time: texture -> tmp
+        a.record(stream)
+        _native.check(lib.rlic_sweep_f32(tex.data_ptr(), uv.data_ptr(), n, n, k.data_ptr(),
+                                         KLEN, uv_code, *bcodes, tmp.data_ptr(), sp, 0))
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    evs = evs[2:]  # first two launches are warm-up
+    pass_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    alg_bytes = n * n * 4 * (3 * KLEN - 1)
+    achieved = alg_bytes / (pass_ms / 1e3) / 1e9
+    peaks_path = REPO / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        peak = float(json.loads(peaks_path.read_text())["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = None
+    tfile = REPO / "profiles" / "sweep_traffic.json"
+    if tfile.exists():
+        try:
+            t = json.loads(tfile.read_text())
+            traffic = float(t["dram_bytes_per_pixel_pass"]) * n * n
+        except Exception:
+            traffic = None
+    del uv, tmp
+
+    # ---- end to end through the public API with pinned host buffers
+    host = {}
+    for name, t in (("texture", tex), ("u", u), ("v", v), ("kernel", k)):
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t)
+        host[name] = h.numpy()
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    kw = dict(kernel=host["kernel"], uv_mode="polarization",
+              boundaries={"x": "periodic", "y": "closed"}, iterations=ITERS)
+    rlic_gb300.convolve(host["texture"], host["u"], host["v"], **kw)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        res = rlic_gb300.convolve(host["texture"], host["u"], host["v"], **kw)
+    torch.cuda.synchronize(dev)
+    e2e_s = dist.max(time.perf_counter() - t0, dev)
+    dist.barrier()
+    e2e_value = dist.world * samples * e2e_steps / e2e_s / 1e9
+    assert res.shape == (n, n)
+
+    line = None
+    if dist.rank == 0:
+        clk = clocks.summary()
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": dist.world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded Fourier modes + point vortices, 1% zero cells)",
+            "config": config(n),
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "e2e": {
+                "value": e2e_value,
+                "unit": UNIT,
+                "h2d_bytes_per_step": int(3 * n * n * 4 + KLEN * 4),
+                "d2h_bytes_per_step": int(n * n * 4),
+                "ms_per_step": 1e3 * e2e_s / e2e_steps,
+                "path": "rlic_gb300.convolve(numpy, pinned) -> rlic_convolve_f32 host-memory",
+            },
+            "roofline": {
+                "bound": "hbm",
+                "kernel": "lic_sweep_kernel<float, fma, branchless, polarization>",
+                "achieved": achieved,
+                "peak": peak,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs, burst)",
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "pass_ms": pass_ms,
+            },
+        }
+        if not args.no_cpu_baseline:
+            from oracle import oracle
+
+            case_np = {x: case[x].cpu().numpy() for x in ("texture", "u", "v", "kernel")}
+            case_np.update(uv_mode="polarization", boundaries={"x": "periodic", "y": "closed"})
+            cb = cpu_sample(case_np, args.cpu_seconds, oracle.env_threads())
+            cb.pop("seconds", None)
+            line["cpu_baseline"] = cb
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main() -> None:
+    args = parse_args()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        return
+    run_gb300(args, dist)
+
+
+if __name__ == "__main__":
+    main()

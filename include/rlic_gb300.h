@@ -1,0 +1,185 @@
+/*
+ * rlic_gb300.h -- C ABI of the GB300 (sm_103a) line integral convolution core.
+ *
+ * This library replaces the native module of neutrinoceros/rlic, whose only
+ * entry points are the PyO3 functions
+ *
+ *     rlic._core.convolve_f32(texture, (u, v, uv_mode), kernel,
+ *                             ((x_left, x_right), (y_left, y_right)), iterations)
+ *     rlic._core.convolve_f64(...)                        (src/lib.rs:448-485,
+ *                                                          src/rlic/_core.pyi:8-29)
+ *
+ * The Python layer (rlic_gb300/_lib.py, mirroring src/rlic/_lib.py:37-235)
+ * validates every argument before it calls into this ABI, exactly as the
+ * reference validates before calling its native module.  This ABI still
+ * checks its arguments and returns an error code instead of aborting.
+ *
+ * Conventions
+ *   - Images are C-order (row-major) arrays of ny rows by nx columns:
+ *     element (i, j) sits at index i * nx + j.  i runs along y (rows, v),
+ *     j along x (columns, u), as in src/lib.rs:47-51.
+ *   - All pointers are CUDA device pointers unless RLIC_FLAG_HOST_MEMORY is
+ *     set, in which case texture, u, v, kernel and out are host pointers and
+ *     the call copies them to and from the device and returns after the result
+ *     is back in `out`.  Without that flag the call is asynchronous on `stream`
+ *     (a cudaStream_t; NULL means the legacy default stream).
+ *   - `out` must not overlap any input.  Inputs are never written.
+ *   - Return value: RLIC_OK or an RLIC_ERR_* code; rlic_last_error() then
+ *     describes the failure (thread-local).
+ *   - Arithmetic reproduces the reference's default build (Cargo features
+ *     `fma` and `branchless`, Cargo.toml:27-30) bit for bit.  The other three
+ *     feature combinations are selected with RLIC_FLAG_NO_FMA and
+ *     RLIC_FLAG_NO_BRANCHLESS.
+ */
+#ifndef RLIC_GB300_H
+#define RLIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define RLIC_API __attribute__((visibility("default")))
+#else
+#define RLIC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define RLIC_OK 0
+#define RLIC_ERR_INVALID_ARGUMENT 1
+#define RLIC_ERR_CUDA 2
+#define RLIC_ERR_OUT_OF_MEMORY 3
+#define RLIC_ERR_WORKSPACE_TOO_SMALL 4
+
+/* uv_mode: src/lib.rs:14-27 ("velocity" / "polarization") */
+#define RLIC_UV_VELOCITY 0
+#define RLIC_UV_POLARIZATION 1
+
+/* boundary kinds: src/lib.rs:56-67 ("closed" / "periodic") */
+#define RLIC_BOUNDARY_CLOSED 0
+#define RLIC_BOUNDARY_PERIODIC 1
+
+/* flags */
+#define RLIC_FLAG_HOST_MEMORY 0x1u   /* array pointers are host memory            */
+#define RLIC_FLAG_NO_FMA 0x2u        /* reference built without feature `fma`       */
+#define RLIC_FLAG_NO_BRANCHLESS 0x4u /* reference built without feature `branchless` */
+
+/* Library version string. */
+RLIC_API const char *rlic_version(void);
+
+/* Description of the last error raised on the calling thread ("" if none). */
+RLIC_API const char *rlic_last_error(void);
+
+/*
+ * Device scratch, in bytes, that rlic_convolve_f32/_f64 need for an image of
+ * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps and
+ * `iterations` passes: the packed (u, v) field and, for two or more
+ * iterations, one ping-pong texture buffer.  0 on invalid arguments.
+ */
+RLIC_API size_t rlic_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int64_t iterations,
+                            int elem_bytes);
+
+/*
+ * Line integral convolution, `iterations` passes.
+ *
+ * Replaces rlic._core.convolve_f32 / convolve_f64 (src/lib.rs:451-482), i.e.
+ * convolve_iteratively (src/lib.rs:408-443): the texture is convolved along
+ * the streamlines of (u, v) with `kernel`, and each pass feeds its output to
+ * the next one.  iterations == 0 writes zeros to `out`, as the native core
+ * does (src/lib.rs:425, 433); the Python layer returns a copy of the texture
+ * instead, before it reaches this call (src/rlic/_lib.py:208-209).
+ *
+ *   texture, u, v   ny x nx, C-order
+ *   kernel          klen taps; the first klen/2 weight the backward half of
+ *                   the streamline, the last klen - klen/2 - 1 the forward half
+ *   uv_mode         RLIC_UV_VELOCITY or RLIC_UV_POLARIZATION
+ *   bx_left, bx_right, by_left, by_right
+ *                   RLIC_BOUNDARY_CLOSED or RLIC_BOUNDARY_PERIODIC for each
+ *                   side of each axis (x = columns, y = rows).  Any
+ *                   combination is computed; the Python layer rejects a
+ *                   periodic side facing a different one.
+ *   out             ny x nx result
+ *   workspace       device scratch of at least rlic_workspace_bytes(...)
+ *                   bytes, 256-byte aligned, or NULL to let the call allocate
+ *                   it stream-ordered (cudaMallocAsync / cudaFreeAsync).
+ *                   Ignored with RLIC_FLAG_HOST_MEMORY (the call allocates).
+ */
+RLIC_API int rlic_convolve_f32(const float *texture, const float *u, const float *v, int64_t ny,
+                      int64_t nx, const float *kernel, int64_t klen, int uv_mode,
+                      int bx_left, int bx_right, int by_left, int by_right,
+                      int64_t iterations, float *out, void *workspace,
+                      size_t workspace_bytes, void *stream, unsigned flags);
+
+RLIC_API int rlic_convolve_f64(const double *texture, const double *u, const double *v,
+                      int64_t ny, int64_t nx, const double *kernel, int64_t klen,
+                      int uv_mode, int bx_left, int bx_right, int by_left, int by_right,
+                      int64_t iterations, double *out, void *workspace,
+                      size_t workspace_bytes, void *stream, unsigned flags);
+
+/*
+ * Streamline cells, for index-for-index parity checks of the trace
+ * (convole_single_pixel, src/lib.rs:305-362; advance, src/lib.rs:236-273).
+ *
+ * For each of the npix pixels whose linear indices (i * nx + j) are in `pix`,
+ * writes klen - 1 linear cell indices to cells[p * (klen - 1) ...]: first the
+ * klen - klen/2 - 1 cells reached by the forward trace, then the klen/2 cells
+ * reached by the backward trace, each slot after a NaN stop set to -1.
+ * Pointers follow RLIC_FLAG_HOST_MEMORY like rlic_convolve_*.
+ */
+RLIC_API int rlic_trace_cells_f32(const float *u, const float *v, int64_t ny, int64_t nx,
+                         int64_t klen, int uv_mode, int bx_left, int bx_right, int by_left,
+                         int by_right, int64_t npix, const int64_t *pix, int64_t *cells,
+                         void *stream, unsigned flags);
+
+RLIC_API int rlic_trace_cells_f64(const double *u, const double *v, int64_t ny, int64_t nx,
+                         int64_t klen, int uv_mode, int bx_left, int bx_right,
+                         int by_left, int by_right, int64_t npix, const int64_t *pix,
+                         int64_t *cells, void *stream, unsigned flags);
+
+/*
+ * Building blocks of rlic_convolve_*, for callers that convolve many
+ * textures over one field (all pointers device memory, asynchronous):
+ *
+ * rlic_pack_field_*: interleave u and v (ny x nx each) into `uv`, an array
+ *   of ny * nx (u, v) pairs (2 * ny * nx elements, aligned to one pair), the
+ *   layout every streamline step reads.  No counterpart in the reference,
+ *   which reads u and v from two views (src/lib.rs:332-335).
+ *
+ * rlic_sweep_*: one convolution pass, `convolve` of src/lib.rs:364-406:
+ *   tex_out = LIC(tex_in) along the packed field.  `flags` takes the
+ *   variant bits only.
+ */
+RLIC_API int rlic_pack_field_f32(const float *u, const float *v, int64_t ny, int64_t nx,
+                                 void *uv, void *stream);
+RLIC_API int rlic_pack_field_f64(const double *u, const double *v, int64_t ny, int64_t nx,
+                                 void *uv, void *stream);
+RLIC_API int rlic_sweep_f32(const float *tex_in, const void *uv, int64_t ny, int64_t nx,
+                            const float *kernel, int64_t klen, int uv_mode, int bx_left,
+                            int bx_right, int by_left, int by_right, float *tex_out,
+                            void *stream, unsigned flags);
+RLIC_API int rlic_sweep_f64(const double *tex_in, const void *uv, int64_t ny, int64_t nx,
+                            const double *kernel, int64_t klen, int uv_mode, int bx_left,
+                            int bx_right, int by_left, int by_right, double *tex_out,
+                            void *stream, unsigned flags);
+
+/*
+ * Launch-shape tuning for the streamline kernels: CTA width and height in
+ * pixels (block_x * block_y threads, at most 256; block_x a multiple of 32
+ * or a divisor of 32).  Affects calls made after it on any thread.
+ */
+RLIC_API int rlic_set_block_shape(int block_x, int block_y);
+
+/*
+ * Number of this library's kernels launched since load (all threads).  Lets
+ * a caller confirm that work ran on the device and count launches per call.
+ */
+RLIC_API uint64_t rlic_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RLIC_GB300_H */

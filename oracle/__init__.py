@@ -1,0 +1,6 @@
+"""CPU oracle of rLIC's convolution (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this package, as the checker; the product package
+``rlic_gb300`` never imports it.
+"""

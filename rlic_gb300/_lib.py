@@ -1,0 +1,269 @@
+"""``convolve``: the drop-in public entry point.
+
+Same signature, dtype rules, validation order and error texts as the
+reference's ``rlic.convolve`` (src/rlic/_lib.py:37-235).  Every input check
+runs first and all failures are collected; one failure is raised as is,
+several are raised together as ``ExceptionGroup("Invalid inputs were
+received.", ...)``.  ``iterations=0`` returns a copy of the texture after
+validation (src/rlic/_lib.py:208-209).  Everything else runs on the GPU
+through the C ABI of ``librlic_gb300.so``; there is no CPU fallback.
+
+Inputs may be numpy arrays (the reference's contract: the result is a new
+numpy array) or torch CUDA tensors (the result is a new tensor on the same
+device, computed on the current torch stream, with no host round trip).
+"""
+
+from __future__ import annotations
+
+__all__ = ["convolve"]
+
+import ctypes
+from typing import TYPE_CHECKING, Any
+
+import numpy as np
+
+from rlic_gb300 import _native
+from rlic_gb300._boundaries import BoundarySet
+
+if TYPE_CHECKING:
+    from rlic_gb300._boundaries import BoundarySpec
+    from rlic_gb300._typing import FArray1D, FArray2D, UVMode
+
+_KNOWN_UV_MODES = ["velocity", "polarization"]
+_SUPPORTED_DTYPES: list[np.dtype[np.floating]] = [
+    np.dtype("float32"),
+    np.dtype("float64"),
+]
+
+
+def _is_torch(x: Any) -> bool:
+    return type(x).__module__.split(".")[0] == "torch"
+
+
+class _Ops:
+    """The few array operations validation needs, for numpy or torch."""
+
+    def __init__(self, use_torch: bool) -> None:
+        self.torch = use_torch
+        if use_torch:
+            import torch
+
+            self._t = torch
+            self.supported = [torch.float32, torch.float64]
+        else:
+            self.supported = _SUPPORTED_DTYPES
+
+    def shape(self, a: Any) -> tuple[int, ...]:
+        return tuple(a.shape)
+
+    def any_negative(self, a: Any) -> bool:
+        if self.torch:
+            return bool((a < 0).any())
+        return bool(np.any(a < 0))
+
+    def any_nonfinite(self, a: Any) -> bool:
+        if self.torch:
+            return bool((~self._t.isfinite(a)).any())
+        return bool(np.any(~np.isfinite(a)))
+
+
+def _collect_problems(
+    ops: _Ops,
+    texture: Any,
+    u: Any,
+    v: Any,
+    kernel: Any,
+    uv_mode: Any,
+    boundaries: Any,
+    iterations: int,
+) -> tuple[list[Exception], BoundarySet | None]:
+    """All validation failures, in the reference's order (src/rlic/_lib.py:135-200)."""
+    problems: list[Exception] = []
+    if iterations < 0:
+        problems.append(
+            ValueError(
+                f"Invalid number of iterations: {iterations}\n"
+                "Expected a strictly positive integer."
+            )
+        )
+    if uv_mode not in _KNOWN_UV_MODES:
+        problems.append(
+            ValueError(f"Invalid uv_mode {uv_mode!r}. Expected one of {_KNOWN_UV_MODES}")
+        )
+
+    expectation = (
+        "Expected texture, u, v and kernel with identical dtype, from "
+        f"{ops.supported}. Got texture.dtype={texture.dtype!r}, u.dtype={u.dtype!r}, "
+        f"v.dtype={v.dtype!r}, kernel.dtype={kernel.dtype!r}"
+    )
+    dtypes = {a.dtype for a in (texture, u, v, kernel)}
+    unsupported = dtypes.difference(ops.supported)
+    if unsupported:
+        problems.append(
+            TypeError(f"Found unsupported data type(s): {list(unsupported)}. {expectation}")
+        )
+    if len(dtypes) != 1:
+        problems.append(TypeError(f"Data types mismatch. {expectation}"))
+
+    if texture.ndim != 2:
+        problems.append(
+            ValueError(f"Expected a texture with exactly two dimensions. Got texture.ndim={texture.ndim!r}")
+        )
+    if ops.any_negative(texture):
+        problems.append(
+            ValueError("Found invalid texture element(s). Expected only positive values.")
+        )
+    tshape, ushape, vshape = ops.shape(texture), ops.shape(u), ops.shape(v)
+    if ushape != tshape or vshape != tshape:
+        problems.append(
+            ValueError(
+                "Shape mismatch: expected texture, u and v with identical shapes. "
+                f"Got texture.shape={tshape!r}, u.shape={ushape!r}, v.shape={vshape!r}"
+            )
+        )
+    if kernel.ndim != 1:
+        problems.append(
+            ValueError(f"Expected a kernel with exactly one dimension. Got kernel.ndim={kernel.ndim!r}")
+        )
+    if ops.any_nonfinite(kernel):
+        problems.append(ValueError("Found non-finite value(s) in kernel."))
+
+    bs = BoundarySet.from_spec(boundaries)
+    if bs is None:
+        problems.append(TypeError(f"Invalid boundary specification {boundaries}"))
+    else:
+        problems.extend(bs.collect_exceptions())
+    return problems, bs
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _convolve_numpy(
+    texture: np.ndarray,
+    u: np.ndarray,
+    v: np.ndarray,
+    kernel: np.ndarray,
+    uv_code: int,
+    bcodes: tuple[int, int, int, int],
+    iterations: int,
+) -> np.ndarray:
+    lib = _native.lib()
+    dtype = texture.dtype
+    tex_c = np.ascontiguousarray(texture)
+    u_c = np.ascontiguousarray(u)
+    v_c = np.ascontiguousarray(v)
+    k_c = np.ascontiguousarray(kernel)
+    out = np.empty(tex_c.shape, dtype=dtype)
+    ny, nx = tex_c.shape
+    fn = lib.rlic_convolve_f32 if dtype == np.dtype("float32") else lib.rlic_convolve_f64
+    rc = fn(
+        _ptr(tex_c), _ptr(u_c), _ptr(v_c), ny, nx, _ptr(k_c), k_c.shape[0], uv_code,
+        *bcodes, iterations, _ptr(out), None, 0, None, _native.RLIC_FLAG_HOST_MEMORY,
+    )
+    _native.check(rc)
+    return out
+
+
+def _convolve_torch(
+    texture: Any,
+    u: Any,
+    v: Any,
+    kernel: Any,
+    uv_code: int,
+    bcodes: tuple[int, int, int, int],
+    iterations: int,
+) -> Any:
+    import torch
+
+    lib = _native.lib()
+    dev = texture.device
+    if dev.type != "cuda" or u.device != dev or v.device != dev:
+        raise ValueError(
+            "torch inputs must be CUDA tensors on one device. "
+            f"Got texture.device={texture.device}, u.device={u.device}, v.device={v.device}"
+        )
+    with torch.cuda.device(dev):
+        tex_c = texture.contiguous()
+        u_c = u.contiguous()
+        v_c = v.contiguous()
+        k_c = kernel.to(device=dev).contiguous()
+        out = torch.empty_like(tex_c, memory_format=torch.contiguous_format)
+        ny, nx = tex_c.shape
+        elem = tex_c.element_size()
+        nbytes = lib.rlic_workspace_bytes(ny, nx, k_c.shape[0], iterations, elem)
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        fn = lib.rlic_convolve_f32 if tex_c.dtype == torch.float32 else lib.rlic_convolve_f64
+        rc = fn(
+            tex_c.data_ptr(), u_c.data_ptr(), v_c.data_ptr(), ny, nx, k_c.data_ptr(),
+            k_c.shape[0], uv_code, *bcodes, iterations, out.data_ptr(), ws.data_ptr(), nbytes,
+            ctypes.c_void_p(stream), 0,
+        )
+        _native.check(rc)
+    return out
+
+
+def convolve(
+    texture: FArray2D,
+    /,
+    u: FArray2D,
+    v: FArray2D,
+    *,
+    kernel: FArray1D,
+    uv_mode: UVMode = "velocity",
+    boundaries: BoundarySpec = "closed",
+    iterations: int = 1,
+) -> FArray2D:
+    """2-dimensional line integral convolution, on the GPU.
+
+    Convolves ``texture`` along the streamlines of the vector field
+    ``(u, v)`` with the 1-D ``kernel``: each output pixel is the
+    kernel-weighted sum of texture samples met while tracing the streamline
+    through that pixel forward (second half of the kernel) and backward
+    (first half of the kernel).
+
+    texture: 2-D array of non-negative values (positional only).
+    u, v: 2-D arrays, the x (column) and y (row) components of the field.
+    kernel: 1-D array of finite weights (keyword only).
+    uv_mode: "velocity" (direction matters) or "polarization" (each sample
+        is flipped to agree with the previous one, so direction is ignored).
+    boundaries: "closed", "periodic", or {"x": spec, "y": spec} with each
+        spec a name or a (left, right) pair; a periodic side must face a
+        periodic side.
+    iterations: number of passes, each fed with the previous output; 0
+        returns a copy of the texture.
+
+    All four arrays share one dtype, float32 or float64.  The result is a
+    new array of that dtype and the inputs are never modified.  numpy inputs
+    give a numpy result; torch CUDA tensors give a tensor on their device.
+
+    Raises TypeError for mismatched or unsupported dtypes, ValueError for
+    other invalid inputs, and an ExceptionGroup when several problems are
+    found at once.  The results, messages and edge cases follow the
+    reference (src/rlic/_lib.py:37-235, src/lib.rs:305-443).
+    """
+    use_torch = _is_torch(texture)
+    ops = _Ops(use_torch)
+    problems, bs = _collect_problems(
+        ops, texture, u, v, kernel, uv_mode, boundaries, iterations
+    )
+    if len(problems) == 1:
+        raise problems[0]
+    if problems:
+        raise ExceptionGroup("Invalid inputs were received.", problems)
+    assert bs is not None
+
+    if iterations == 0:
+        return texture.clone() if use_torch else texture.copy()
+
+    uv_code = _native.UV_MODE_CODES[uv_mode]
+    bcodes = bs.codes()
+    if use_torch:
+        if not all(_is_torch(a) for a in (u, v, kernel)):
+            raise TypeError("texture is a torch tensor: u, v and kernel must be tensors too")
+        return _convolve_torch(texture, u, v, kernel, uv_code, bcodes, iterations)
+    if any(_is_torch(a) for a in (u, v, kernel)):
+        raise TypeError("texture is a numpy array: u, v and kernel must be numpy arrays too")
+    return _convolve_numpy(texture, u, v, kernel, uv_code, bcodes, iterations)

@@ -1,0 +1,114 @@
+"""ctypes binding of ``librlic_gb300.so`` (C ABI in ``include/rlic_gb300.h``).
+
+The shared library is built in-tree by ``rlic_gb300._build`` (or
+``__graft_entry__.build()``).  There is no fallback: when the library is
+missing or cannot be loaded, every call that needs it raises
+``NativeLibraryError``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().with_name("librlic_gb300.so")
+
+RLIC_OK = 0
+RLIC_ERR_INVALID_ARGUMENT = 1
+RLIC_ERR_CUDA = 2
+RLIC_ERR_OUT_OF_MEMORY = 3
+RLIC_ERR_WORKSPACE_TOO_SMALL = 4
+
+RLIC_UV_VELOCITY = 0
+RLIC_UV_POLARIZATION = 1
+
+RLIC_FLAG_HOST_MEMORY = 0x1
+RLIC_FLAG_NO_FMA = 0x2
+RLIC_FLAG_NO_BRANCHLESS = 0x4
+
+UV_MODE_CODES: dict[str, int] = {
+    "velocity": RLIC_UV_VELOCITY,
+    "polarization": RLIC_UV_POLARIZATION,
+}
+
+# Every symbol the header declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_INT = ctypes.c_int
+_SZ = ctypes.c_size_t
+_U = ctypes.c_uint
+_CONVOLVE_ARGS = [_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _I64, _P, _P,
+                  _SZ, _P, _U]
+_TRACE_ARGS = [_P, _P, _I64, _I64, _I64, _INT, _INT, _INT, _INT, _INT, _I64, _P, _P, _P, _U]
+SIGNATURES: dict[str, tuple[list, object]] = {
+    "rlic_version": ([], ctypes.c_char_p),
+    "rlic_last_error": ([], ctypes.c_char_p),
+    "rlic_workspace_bytes": ([_I64, _I64, _I64, _I64, _INT], _SZ),
+    "rlic_convolve_f32": (_CONVOLVE_ARGS, _INT),
+    "rlic_convolve_f64": (_CONVOLVE_ARGS, _INT),
+    "rlic_trace_cells_f32": (_TRACE_ARGS, _INT),
+    "rlic_trace_cells_f64": (_TRACE_ARGS, _INT),
+    "rlic_pack_field_f32": ([_P, _P, _I64, _I64, _P, _P], _INT),
+    "rlic_pack_field_f64": ([_P, _P, _I64, _I64, _P, _P], _INT),
+    "rlic_sweep_f32": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _U],
+                       _INT),
+    "rlic_sweep_f64": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _U],
+                       _INT),
+    "rlic_set_block_shape": ([_INT, _INT], _INT),
+    "rlic_kernel_launch_count": ([], ctypes.c_uint64),
+}
+
+
+class NativeLibraryError(RuntimeError):
+    """The native library is missing, failed to load, or a call failed."""
+
+    def __init__(self, message: str, code: int | None = None) -> None:
+        super().__init__(message)
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded library (loaded on first use)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise NativeLibraryError(
+                    f"{LIB_PATH.name} is not built: run `python -m rlic_gb300._build` "
+                    "(needs nvcc) before using rlic_gb300"
+                )
+            try:
+                handle = ctypes.CDLL(str(LIB_PATH))
+            except OSError as exc:
+                raise NativeLibraryError(f"cannot load {LIB_PATH}: {exc}") from exc
+            for name, (argtypes, restype) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.argtypes = argtypes
+                fn.restype = restype
+            _lib = handle
+    return _lib
+
+
+def check(code: int) -> None:
+    """Raise NativeLibraryError for a non-zero status code."""
+    if code != RLIC_OK:
+        msg = lib().rlic_last_error().decode(errors="replace")
+        if code == RLIC_ERR_OUT_OF_MEMORY:
+            raise MemoryError(f"rlic_gb300: {msg}")
+        raise NativeLibraryError(f"rlic_gb300 error {code}: {msg}", code)
+
+
+def launch_count() -> int:
+    """Kernels this library has launched since it was loaded."""
+    return int(lib().rlic_kernel_launch_count())
+
+
+def set_block_shape(block_x: int, block_y: int) -> None:
+    check(lib().rlic_set_block_shape(block_x, block_y))

@@ -1,0 +1,92 @@
+"""The C ABI library loads, exports every declared symbol, and rejects bad
+arguments with status codes -- all without touching a GPU (argument checks
+run before any CUDA call)."""
+
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+import pytest
+
+from rlic_gb300 import _native
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "rlic_gb300.h"
+
+
+def declared_symbols() -> list[str]:
+    text = HEADER.read_text()
+    return re.findall(r"RLIC_API\s+[\w\s\*]+?\b(rlic_\w+)\s*\(", text)
+
+
+def test_header_declares_the_binding_table() -> None:
+    assert sorted(declared_symbols()) == sorted(_native.SIGNATURES)
+
+
+def test_library_exports_every_declared_symbol(native) -> None:
+    for name in declared_symbols():
+        assert hasattr(native, name), name
+
+
+def test_version(native) -> None:
+    assert native.rlic_version().decode().startswith("rlic_gb300")
+
+
+def test_workspace_bytes(native) -> None:
+    ws = native.rlic_workspace_bytes
+    # packed (u, v) + kernel copy; + ping-pong buffer from two iterations on
+    assert ws(8192, 8192, 65, 1, 4) == 2 * 8192 * 8192 * 4 + 512
+    assert ws(8192, 8192, 65, 5, 4) == 3 * 8192 * 8192 * 4 + 512
+    assert ws(10, 10, 3, 2, 8) == 1792 + 1024 + 256
+    assert ws(0, 10, 3, 1, 4) == 0
+    assert ws(10, 10, 3, 1, 2) == 0
+
+
+def _call(native, **over):
+    args = dict(texture=1, u=1, v=1, ny=4, nx=4, kernel=1, klen=3, uv_mode=0, bxl=0, bxr=0,
+                byl=0, byr=0, iterations=1, out=1, ws=None, wsb=0, stream=None, flags=0)
+    args.update(over)
+    return native.rlic_convolve_f32(*args.values())
+
+
+@pytest.mark.parametrize(
+    "over, text",
+    [
+        (dict(ny=0), "dimensions"),
+        (dict(nx=-3), "dimensions"),
+        (dict(klen=0), "at least one tap"),
+        (dict(uv_mode=2), "uv_mode"),
+        (dict(bxr=2), "boundaries"),
+        (dict(iterations=-1), "iterations"),
+        (dict(texture=None), "null"),
+        (dict(flags=0x100), "flag"),
+    ],
+)
+def test_argument_errors(native, over, text) -> None:
+    rc = _call(native, **over)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert text in native.rlic_last_error().decode()
+
+
+def test_check_raises(native) -> None:
+    _call(native, ny=0)
+    with pytest.raises(_native.NativeLibraryError, match="dimensions"):
+        _native.check(_native.RLIC_ERR_INVALID_ARGUMENT)
+
+
+def test_trace_argument_errors(native) -> None:
+    rc = native.rlic_trace_cells_f64(1, 1, 4, 4, 3, 0, 0, 0, 0, 0, -1, 1, 1, None, 0)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+
+
+def test_block_shape_validation(native) -> None:
+    assert native.rlic_set_block_shape(0, 4) == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert native.rlic_set_block_shape(64, 64) == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert native.rlic_set_block_shape(32, 8) == _native.RLIC_OK
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path) -> None:
+    monkeypatch.setattr(_native, "_lib", None)
+    monkeypatch.setattr(_native, "LIB_PATH", tmp_path / "librlic_gb300.so")
+    with pytest.raises(_native.NativeLibraryError, match="not built"):
+        _native.lib()

@@ -1,0 +1,334 @@
+"""Bit-exact parity of the CUDA path with the oracle, through the C ABI.
+
+The bar is bit-exact output (integer-exact streamline cells, identical
+floating-point outputs): the device arithmetic reproduces every rounding of
+the reference (src/lib.rs:157-406).  Cases cover the committed golden
+vectors, the README workload, random fields with zeros / signed zeros /
+NaNs / infinities, degenerate images, short, even and over-long kernels,
+every boundary combination, both uv modes, several iterations and all four
+Cargo feature variants.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import zlib
+from itertools import product
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import rlic_gb300
+from rlic_gb300 import _native
+from rlic_gb300.workloads import fourier_vortex_case, readme_case
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CODES = {"closed": 0, "periodic": 1}
+
+
+def _codes(bnd):
+    if isinstance(bnd, str):
+        return (CODES[bnd],) * 4
+    if isinstance(bnd, dict):
+        def pair(b):
+            return (b, b) if isinstance(b, str) else tuple(b)
+        bnd = (pair(bnd["x"]), pair(bnd["y"]))
+    (xl, xr), (yl, yr) = bnd
+    return tuple(CODES[b] for b in (xl, xr, yl, yr))
+
+
+def _variant_flags(variant: int) -> int:
+    flags = 0
+    if not variant & 1:
+        flags |= _native.RLIC_FLAG_NO_FMA
+    if not variant & 2:
+        flags |= _native.RLIC_FLAG_NO_BRANCHLESS
+    return flags
+
+
+def capi_convolve(tex, u, v, k, uv_mode="velocity", boundaries="closed", iterations=1,
+                  variant=3):
+    """rlic_convolve_* with host buffers (the call copies in and out)."""
+    lib = _native.lib()
+    dtype = np.asarray(tex).dtype
+    tex, u, v, k = (np.ascontiguousarray(a, dtype=dtype) for a in (tex, u, v, k))
+    out = np.full(tex.shape, np.nan, dtype=dtype)
+    fn = lib.rlic_convolve_f32 if dtype == np.float32 else lib.rlic_convolve_f64
+    ny, nx = tex.shape
+    rc = fn(tex.ctypes.data, u.ctypes.data, v.ctypes.data, ny, nx, k.ctypes.data, k.size,
+            int(uv_mode == "polarization"), *_codes(boundaries), iterations, out.ctypes.data,
+            None, 0, None, _native.RLIC_FLAG_HOST_MEMORY | _variant_flags(variant))
+    _native.check(rc)
+    return out
+
+
+def capi_cells(u, v, klen, pix, uv_mode="velocity", boundaries="closed", variant=3):
+    lib = _native.lib()
+    dtype = np.asarray(u).dtype
+    u, v = (np.ascontiguousarray(a, dtype=dtype) for a in (u, v))
+    pix = np.ascontiguousarray(pix, dtype=np.int64)
+    cells = np.full((pix.size, max(klen - 1, 0)), -7, dtype=np.int64)
+    fn = lib.rlic_trace_cells_f32 if dtype == np.float32 else lib.rlic_trace_cells_f64
+    ny, nx = u.shape
+    rc = fn(u.ctypes.data, v.ctypes.data, ny, nx, klen, int(uv_mode == "polarization"),
+            *_codes(boundaries), pix.size, pix.ctypes.data, cells.ctypes.data, None,
+            _native.RLIC_FLAG_HOST_MEMORY | _variant_flags(variant))
+    _native.check(rc)
+    return cells
+
+
+def assert_bitwise(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.dtype == b.dtype and a.shape == b.shape
+    ia = a.view(np.uint32 if a.dtype == np.float32 else np.uint64)
+    ib = b.view(np.uint32 if b.dtype == np.float32 else np.uint64)
+    # NaN payloads differ between CPU architectures and the GPU: any NaN matches any NaN
+    bad = np.flatnonzero((ia != ib) & ~(np.isnan(a) & np.isnan(b)))
+    assert bad.size == 0, (
+        f"{bad.size} of {a.size} elements differ; first at {np.unravel_index(bad[0], a.shape)}: "
+        f"{a.ravel()[bad[0]]!r} vs {b.ravel()[bad[0]]!r}"
+    )
+
+
+# ------------------------------------------------------------- golden --
+
+@pytest.mark.parametrize("path", sorted(GOLDEN.glob("*.npz")), ids=lambda p: p.stem)
+def test_golden_vectors(path) -> None:
+    g = np.load(path, allow_pickle=False)
+    bnd = ((str(g["bx"][0]), str(g["bx"][1])), (str(g["by"][0]), str(g["by"][1])))
+    out = capi_convolve(g["texture"], g["u"], g["v"], g["kernel"], str(g["uv_mode"]), bnd,
+                        int(g["iterations"]), int(g["variant"]))
+    assert_bitwise(out, g["out"])
+    cells = capi_cells(g["u"], g["v"], g["kernel"].size, g["pix"], str(g["uv_mode"]), bnd,
+                       int(g["variant"]))
+    np.testing.assert_array_equal(cells, g["cells"])
+
+
+# ------------------------------------------------------- README case --
+
+def test_readme_case_output_and_every_path(oracle) -> None:
+    c = readme_case()
+    want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"],
+                           boundaries=c["boundaries"])
+    got = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                              boundaries=c["boundaries"])
+    assert_bitwise(got, want)
+    pix = np.arange(256 * 256)
+    cells = capi_cells(c["u"], c["v"], 65, pix, boundaries="periodic")
+    np.testing.assert_array_equal(cells, oracle.paths(c["u"], c["v"], 65, pix,
+                                                      boundaries="periodic"))
+
+
+# ----------------------------------------------------- random fields --
+
+def _field(rng, ny, nx, dtype, kind):
+    u = (rng.random((ny, nx)) - 0.5).astype(dtype)
+    v = (rng.random((ny, nx)) - 0.5).astype(dtype)
+    if kind == "specials":
+        m = rng.random((ny, nx))
+        u[m < 0.05] = 0.0
+        v[m < 0.05] = 0.0
+        u[(m > 0.05) & (m < 0.08)] = -0.0
+        v[(m > 0.10) & (m < 0.12)] = 0.0
+        v[(m > 0.12) & (m < 0.13)] = -0.0
+        u[(m > 0.20) & (m < 0.205)] = np.nan
+        v[(m > 0.30) & (m < 0.302)] = np.inf
+        u[(m > 0.40) & (m < 0.402)] = -np.inf
+        u[(m > 0.50) & (m < 0.52)] = np.finfo(dtype).tiny / 4  # subnormal
+        v[(m > 0.60) & (m < 0.62)] = 1e30 if dtype == np.float32 else 1e300
+    elif kind == "axis":
+        # exact axis-aligned and diagonal flows exercise ties (tx == ty)
+        u = np.where(rng.random((ny, nx)) < 0.5, 1.0, -1.0).astype(dtype)
+        v = np.where(rng.random((ny, nx)) < 0.3, u, 0.0).astype(dtype)
+    return u, v
+
+
+BOUNDS = [
+    "closed", "periodic", {"x": "periodic", "y": "closed"}, {"x": "closed", "y": "periodic"},
+    # mixed sides: rejected by the Python layer, computed by the native core
+    {"x": ("closed", "periodic"), "y": ("periodic", "closed")},
+]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("uv_mode", ["velocity", "polarization"])
+@pytest.mark.parametrize("bnd", BOUNDS, ids=lambda b: str(b).replace(" ", ""))
+@pytest.mark.parametrize("kind", ["random", "specials", "axis"])
+def test_random_fields(oracle, dtype, uv_mode, bnd, kind) -> None:
+    rng = np.random.default_rng(zlib.crc32(f"{dtype}{uv_mode}{bnd}{kind}".encode()))
+    ny, nx = 37, 53
+    u, v = _field(rng, ny, nx, dtype, kind)
+    tex = rng.random((ny, nx)).astype(dtype)
+    k = rng.random(31).astype(dtype)
+    want = oracle.convolve(tex, u, v, k, uv_mode=uv_mode, boundaries=bnd, iterations=2)
+    got = capi_convolve(tex, u, v, k, uv_mode, bnd, iterations=2)
+    assert_bitwise(got, want)
+    pix = np.arange(ny * nx)
+    np.testing.assert_array_equal(
+        capi_cells(u, v, 31, pix, uv_mode, bnd),
+        oracle.paths(u, v, 31, pix, uv_mode=uv_mode, boundaries=bnd),
+    )
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_feature_variants(oracle, variant, dtype) -> None:
+    rng = np.random.default_rng(100 + variant)
+    u, v = _field(rng, 41, 29, dtype, "specials")
+    tex = rng.random((41, 29)).astype(dtype)
+    k = np.hanning(25).astype(dtype)
+    for mode in ("velocity", "polarization"):
+        want = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries="periodic",
+                               iterations=2, variant=variant)
+        got = capi_convolve(tex, u, v, k, mode, "periodic", 2, variant)
+        assert_bitwise(got, want)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (2, 2), (3, 130), (130, 3)])
+@pytest.mark.parametrize("klen", [1, 2, 3, 4, 5, 64, 65, 301])
+def test_degenerate_shapes_and_kernels(oracle, shape, klen) -> None:
+    rng = np.random.default_rng(sum(shape) * 1000 + klen)
+    u, v = _field(rng, *shape, np.float64, "specials")
+    tex = rng.random(shape)
+    k = rng.random(klen)
+    for bnd, mode in product(["closed", "periodic"], ["velocity", "polarization"]):
+        want = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries=bnd, iterations=3)
+        got = capi_convolve(tex, u, v, k, mode, bnd, iterations=3)
+        assert_bitwise(got, want)
+
+
+@pytest.mark.parametrize("iterations", [0, 1, 2, 3, 4])
+def test_iteration_counts(oracle, iterations) -> None:
+    rng = np.random.default_rng(iterations)
+    u, v = _field(rng, 33, 35, np.float32, "random")
+    tex = rng.random((33, 35)).astype(np.float32)
+    k = np.hanning(17).astype(np.float32)
+    want = oracle.convolve(tex, u, v, k, uv_mode="polarization", iterations=iterations)
+    got = capi_convolve(tex, u, v, k, "polarization", "closed", iterations)
+    assert_bitwise(got, want)  # iterations == 0: zeros, as the native core
+
+
+def test_uniform_fields(oracle) -> None:
+    for uu, vv in [(0.0, 0.0), (np.nan, np.nan), (1.0, 0.0), (0.0, -1.0), (1.0, 1.0),
+                   (-0.0, -0.0), (3.0, -3.0), (np.inf, 1.0)]:
+        u = np.full((20, 21), uu)
+        v = np.full((20, 21), vv)
+        tex = np.random.default_rng(5).random((20, 21))
+        k = np.linspace(0.5, 1, 15)
+        for bnd in ("closed", "periodic"):
+            want = oracle.convolve(tex, u, v, k, boundaries=bnd, iterations=2)
+            assert_bitwise(capi_convolve(tex, u, v, k, "velocity", bnd, 2), want)
+
+
+# --------------------------------------------------- at-scale workload --
+
+def test_fourier_vortex_1024_full(oracle) -> None:
+    c = fourier_vortex_case(n=1024, device="cuda", iterations=2)
+    want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], uv_mode=c["uv_mode"],
+                           boundaries=c["boundaries"], iterations=2,
+                           nthreads=oracle.env_threads())
+    got = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                              uv_mode=c["uv_mode"], boundaries=c["boundaries"], iterations=2)
+    assert_bitwise(got, want)
+
+
+def test_fourier_vortex_full_size_properties(oracle) -> None:
+    """8192^2 float32, K=65, 5 iterations: too large for the oracle in full,
+    so: (1) the first pass of sampled row bands equals the oracle's rows;
+    (2) sampled pixels' streamline cells equal the oracle's; (3) five
+    iterations equal five chained single passes, bit for bit."""
+    import torch
+
+    c = fourier_vortex_case(n=8192, device="cuda", as_numpy=False)
+    tex, u, v, k = c["texture"], c["u"], c["v"], c["kernel"]
+    kw = dict(kernel=k, uv_mode=c["uv_mode"], boundaries=c["boundaries"])
+    one = rlic_gb300.convolve(tex, u, v, iterations=1, **kw)
+    un, vn, tn, kn = (a.cpu().numpy() for a in (u, v, tex, k))
+    onen = one.cpu().numpy()
+    for r0 in (0, 4093, 8192 - 6):
+        rows = oracle.sweep_rows(tn, un, vn, kn, r0, r0 + 6, uv_mode=c["uv_mode"],
+                                 boundaries=c["boundaries"], nthreads=oracle.env_threads())
+        assert_bitwise(onen[r0:r0 + 6], rows)
+    rng = np.random.default_rng(11)
+    pix = rng.integers(0, 8192 * 8192, size=20000)
+    np.testing.assert_array_equal(
+        capi_cells(un, vn, 65, pix, c["uv_mode"], c["boundaries"]),
+        oracle.paths(un, vn, 65, pix, uv_mode=c["uv_mode"], boundaries=c["boundaries"]),
+    )
+    five = rlic_gb300.convolve(tex, u, v, iterations=5, **kw)
+    chain = one
+    for _ in range(4):
+        chain = rlic_gb300.convolve(chain, u, v, iterations=1, **kw)
+    assert torch.equal(five.view(torch.int32), chain.view(torch.int32))
+
+
+# ------------------------------------------------- public API / torch --
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_torch_and_numpy_paths_agree(dtype) -> None:
+    import torch
+
+    rng = np.random.default_rng(9)
+    u, v = _field(rng, 64, 80, dtype, "specials")
+    tex = rng.random((64, 80)).astype(dtype)
+    k = np.hanning(21).astype(dtype)
+    kw = dict(uv_mode="polarization", boundaries={"x": "closed", "y": "periodic"}, iterations=3)
+    a = rlic_gb300.convolve(tex, u, v, kernel=k, **kw)
+    t = [torch.from_numpy(x).cuda() for x in (tex, u, v)]
+    b = rlic_gb300.convolve(*t[:1], t[1], t[2], kernel=torch.from_numpy(k).cuda(), **kw)
+    assert b.is_cuda and b.dtype == t[0].dtype
+    assert_bitwise(a, b.cpu().numpy())
+
+
+def test_strided_and_broadcast_inputs(oracle) -> None:
+    c = readme_case(n=96)
+    tex_f = np.asfortranarray(c["texture"])
+    got = rlic_gb300.convolve(tex_f, c["u"], c["v"], kernel=c["kernel"][::-1][::-1],
+                              boundaries="periodic")
+    want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], boundaries="periodic")
+    assert_bitwise(got, want)
+
+
+def test_launches_are_counted() -> None:
+    before = _native.launch_count()
+    c = readme_case(n=64)
+    rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
+    assert _native.launch_count() - before == 4  # pack + 3 passes
+
+
+def test_device_entry_points_with_workspace(oracle) -> None:
+    """rlic_convolve_f32 on device pointers with a caller workspace, and the
+    pack + sweep building blocks, on a torch stream."""
+    import torch
+
+    lib = _native.lib()
+    rng = np.random.default_rng(21)
+    u, v = _field(rng, 70, 90, np.float32, "specials")
+    tex = rng.random((70, 90)).astype(np.float32)
+    k = np.hanning(33).astype(np.float32)
+    want1 = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries="periodic")
+    want3 = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries="periodic",
+                            iterations=3)
+    d = {n: torch.from_numpy(a).cuda() for n, a in dict(t=tex, u=u, v=v, k=k).items()}
+    out = torch.empty_like(d["t"])
+    nbytes = lib.rlic_workspace_bytes(70, 90, 33, 3, 4)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _native.check(lib.rlic_convolve_f32(
+        d["t"].data_ptr(), d["u"].data_ptr(), d["v"].data_ptr(), 70, 90, d["k"].data_ptr(), 33,
+        1, 1, 1, 1, 1, 3, out.data_ptr(), ws.data_ptr(), nbytes, stream, 0))
+    assert_bitwise(out.cpu().numpy(), want3)
+    rc = lib.rlic_convolve_f32(
+        d["t"].data_ptr(), d["u"].data_ptr(), d["v"].data_ptr(), 70, 90, d["k"].data_ptr(), 33,
+        1, 1, 1, 1, 1, 3, out.data_ptr(), ws.data_ptr(), nbytes - 1, stream, 0)
+    assert rc == _native.RLIC_ERR_WORKSPACE_TOO_SMALL
+    uv = torch.empty((70, 90, 2), dtype=torch.float32, device="cuda")
+    _native.check(lib.rlic_pack_field_f32(d["u"].data_ptr(), d["v"].data_ptr(), 70, 90,
+                                          uv.data_ptr(), stream))
+    _native.check(lib.rlic_sweep_f32(d["t"].data_ptr(), uv.data_ptr(), 70, 90,
+                                     d["k"].data_ptr(), 33, 1, 1, 1, 1, 1, out.data_ptr(),
+                                     stream, 0))
+    assert_bitwise(out.cpu().numpy(), want1)
