@@ -5,14 +5,18 @@ float32, 65-tap Hann kernel, polarization mode, boundaries
 {x: periodic, y: closed}, 5 iterations (rlic_gb300.workloads.
 fourier_vortex_case).  Metric: Gsamples/s = H * W * K * iterations / time.
 
-  value     device-resident inputs, rlic_convolve_f32 on device pointers
-            (pack + 5 passes per step), CUDA events on the launching stream;
+  value     device-resident inputs, rlic_convolve_f32 on device pointers in
+            its default (path-cache) form: pack, one traced pass that records
+            every streamline step, four replayed passes; CUDA events on the
+            launching stream.  "forms" also gives the plain form (every pass
+            traced, RLIC_FLAG_NO_PATH_CACHE) on the same workload;
   e2e       the public API rlic_gb300.convolve on host (pinned) numpy
             arrays: validation, host->device copies, compute, device->host
             copy of the result, all inside the timed region;
-  roofline  the dominant kernel (one convolution pass) timed per launch:
-            algorithmic bytes s*(3K-1) per pixel per pass over its duration,
-            against the measured HBM copy bandwidth;
+  roofline  the kernel with the largest share of a step, timed per launch:
+            its algorithmic bytes per pixel (cache-less gather model) over
+            its duration, against the measured HBM copy bandwidth; "kernels"
+            lists every kernel of the step the same way;
   cpu_baseline  the CPU oracle (a restatement of the reference's Rust
             core) timed on a bounded band of rows of the same workload.
 
@@ -74,7 +78,7 @@ def config(n: int) -> dict:
         "uv_mode": "polarization",
         "boundaries": {"x": "periodic", "y": "closed"},
         "iterations": ITERS,
-        "form": "plain (one thread per pixel, packed (u,v), L1-cached gathers)",
+        "form": "path cache (pass 1 traces and records 4-bit step codes, passes 2-5 replay)",
         "l2": "inputs larger than L2 (texture 256 MiB, packed field 512 MiB at 8192^2)",
     }
 
@@ -281,7 +285,7 @@ def run_gb300(args, dist: Dist) -> None:
     uv_code = 1
     samples = n * n * KLEN * ITERS
     out = torch.empty_like(tex)
-    nbytes = lib.rlic_workspace_bytes(n, n, KLEN, ITERS, 4)
+    nbytes = lib.rlic_workspace_bytes(n, n, KLEN, ITERS, 4, 0)
     ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
@@ -316,38 +320,90 @@ def run_gb300(args, dist: Dist) -> None:
     ms_step = ms_total / args.steps
     value = dist.world * samples * args.steps / (ms_total / 1e3) / 1e9
 
-    # ---- dominant kernel: one pass, timed per launch on the same stream
+    # ---- the plain form (every pass traced) on the same workload
+    plain_steps = max(3, min(args.steps, 8))
+    flags_plain = _native.RLIC_FLAG_NO_PATH_CACHE
+
+    def step_plain() -> None:
+        _native.check(lib.rlic_convolve_f32(
+            tex.data_ptr(), u.data_ptr(), v.data_ptr(), n, n, k.data_ptr(), KLEN, uv_code,
+            *bcodes, ITERS, out.data_ptr(), ws.data_ptr(), nbytes, sp, flags_plain))
+
+    step_plain()
+    torch.cuda.synchronize(dev)
+    ev0.record(stream)
+    for _ in range(plain_steps):
+        step_plain()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_ms = dist.max(ev0.elapsed_time(ev1), dev) / plain_steps
+    plain_value = dist.world * samples / (plain_ms / 1e3) / 1e9
+
+    # ---- per-kernel timing on the launching stream (each launch bracketed)
     uv = torch.empty((n, n, 2), dtype=torch.float32, device=dev)
     _native.check(lib.rlic_pack_field_f32(u.data_ptr(), v.data_ptr(), n, n, uv.data_ptr(), sp))
+    codes = torch.empty(lib.rlic_path_code_bytes(n, n, KLEN), dtype=torch.uint8, device=dev)
     tmp = torch.empty_like(tex)
-    passes = max(6, args.steps)
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(passes + 2)]
-    for a, b in evs:  # same pure pass each time: texture -> tmp
-        a.record(stream)
-        _native.check(lib.rlic_sweep_f32(tex.data_ptr(), uv.data_ptr(), n, n, k.data_ptr(),
-                                         KLEN, uv_code, *bcodes, tmp.data_ptr(), sp, 0))
-        b.record(stream)
-    torch.cuda.synchronize(dev)
-    evs = evs[2:]  # first two launches are warm-up
-    pass_ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
-    alg_bytes = n * n * 4 * (3 * KLEN - 1)
-    achieved = alg_bytes / (pass_ms / 1e3) / 1e9
+    reps = max(6, min(args.steps, 12))
+
+    def timed(launch) -> float:
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(reps + 2)]
+        for a, b in evs:
+            a.record(stream)
+            launch()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return statistics.mean(a.elapsed_time(b) for a, b in evs[2:])
+
+    def sweep(code_ptr):
+        return lambda: _native.check(lib.rlic_sweep_f32(
+            tex.data_ptr(), uv.data_ptr(), n, n, k.data_ptr(), KLEN, uv_code, *bcodes,
+            tmp.data_ptr(), code_ptr, sp, 0))
+
+    ms_trace_rec = timed(sweep(codes.data_ptr()))
+    ms_trace = timed(sweep(None))
+    ms_replay = timed(lambda: _native.check(lib.rlic_replay_f32(
+        tex.data_ptr(), codes.data_ptr(), n, n, k.data_ptr(), KLEN, tmp.data_ptr(), sp, 0)))
+    ms_pack = timed(lambda: _native.check(lib.rlic_pack_field_f32(
+        u.data_ptr(), v.data_ptr(), n, n, uv.data_ptr(), sp)))
+    del uv, tmp, codes
+
     peaks_path = REPO / "MEASURED_PEAKS.json"
     if peaks_path.exists():
         peak = float(json.loads(peaks_path.read_text())["hbm_gbs"])
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
+    px = n * n
+    code_b = lib.rlic_path_code_bytes(n, n, KLEN) / px
+    # algorithmic bytes per pixel of each kernel (cache-less gather model)
+    alg = {
+        "trace_record": 4 * (3 * KLEN - 1) + code_b,  # u, v, tex per step + centre + out + codes
+        "trace": 4 * (3 * KLEN - 1),
+        "replay": code_b + 4 * KLEN + 4,              # codes + tex per tap + out
+        "pack": 16,                                    # u, v in, (u, v) out
+    }
+    times = {"trace_record": ms_trace_rec, "trace": ms_trace, "replay": ms_replay,
+             "pack": ms_pack}
+    kernels = {}
+    for name, ms in times.items():
+        gbs = alg[name] * px / (ms / 1e3) / 1e9
+        kernels[name] = {"ms": ms, "alg_bytes_per_px": alg[name], "achieved_gbs": gbs,
+                         "frac": gbs / peak}
+    per_step = {"trace_record": ms_trace_rec, "replay": (ITERS - 1) * ms_replay,
+                "pack": ms_pack}
+    dominant = max(per_step, key=per_step.get)
+    for name, ms in per_step.items():
+        kernels[name]["share_of_step"] = ms / sum(per_step.values())
     traffic = None
-    tfile = REPO / "profiles" / "sweep_traffic.json"
+    tfile = REPO / "profiles" / "traffic.json"
     if tfile.exists():
         try:
             t = json.loads(tfile.read_text())
-            traffic = float(t["dram_bytes_per_pixel_pass"]) * n * n
+            traffic = float(t[dominant]["dram_bytes_per_px"]) * px
         except Exception:
             traffic = None
-    del uv, tmp
 
     # ---- end to end through the public API with pinned host buffers
     host = {}
@@ -399,15 +455,22 @@ def run_gb300(args, dist: Dist) -> None:
             },
             "roofline": {
                 "bound": "hbm",
-                "kernel": "lic_sweep_kernel<float, fma, branchless, polarization>",
-                "achieved": achieved,
+                "kernel": {"trace_record": "lic_pass_kernel<float, fma, branchless, pol, record>",
+                           "replay": "lic_gather_kernel<float, fma>",
+                           "pack": "pack_uv_kernel<float>"}[dominant],
+                "achieved": kernels[dominant]["achieved_gbs"],
                 "peak": peak,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs, burst)",
                 "unit": "GB/s",
-                "frac": achieved / peak,
+                "frac": kernels[dominant]["frac"],
                 "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "pass_ms": pass_ms,
+                "algorithmic_bytes_per_launch": alg[dominant] * px,
+                "launch_ms": times[dominant],
+            },
+            "kernels": kernels,
+            "forms": {
+                "path_cache": {"value": value, "ms_per_step": ms_step},
+                "plain": {"value": plain_value, "ms_per_step": plain_ms},
             },
         }
         if not args.no_cpu_baseline:

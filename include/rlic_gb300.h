@@ -66,6 +66,7 @@ extern "C" {
 #define RLIC_FLAG_HOST_MEMORY 0x1u   /* array pointers are host memory            */
 #define RLIC_FLAG_NO_FMA 0x2u        /* reference built without feature `fma`       */
 #define RLIC_FLAG_NO_BRANCHLESS 0x4u /* reference built without feature `branchless` */
+#define RLIC_FLAG_NO_PATH_CACHE 0x8u /* trace every streamline in every pass          */
 
 /* Library version string. */
 RLIC_API const char *rlic_version(void);
@@ -75,12 +76,21 @@ RLIC_API const char *rlic_last_error(void);
 
 /*
  * Device scratch, in bytes, that rlic_convolve_f32/_f64 need for an image of
- * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps and
- * `iterations` passes: the packed (u, v) field and, for two or more
- * iterations, one ping-pong texture buffer.  0 on invalid arguments.
+ * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps,
+ * `iterations` passes and the given flags: the packed (u, v) field, for two
+ * or more iterations one ping-pong texture buffer and (unless
+ * RLIC_FLAG_NO_PATH_CACHE) the path cache, and a copy of the kernel.
+ * 0 on invalid arguments.
  */
 RLIC_API size_t rlic_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int64_t iterations,
-                            int elem_bytes);
+                                     int elem_bytes, unsigned flags);
+
+/*
+ * Bytes of the path cache of an ny x nx image and a kernel of klen taps:
+ * 4 bits per streamline step, 8 steps per 32-bit word, each half of the
+ * kernel padded to whole words.
+ */
+RLIC_API size_t rlic_path_code_bytes(int64_t ny, int64_t nx, int64_t klen);
 
 /*
  * Line integral convolution, `iterations` passes.
@@ -102,6 +112,12 @@ RLIC_API size_t rlic_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int64
  *                   combination is computed; the Python layer rejects a
  *                   periodic side facing a different one.
  *   out             ny x nx result
+ *   flags           RLIC_FLAG_* bits.  With two or more iterations the first
+ *                   pass records every streamline step (4 bits each) and the
+ *                   later passes replay the record instead of re-tracing
+ *                   (the path of a pixel depends on u, v and the kernel
+ *                   length only); RLIC_FLAG_NO_PATH_CACHE traces every pass.
+ *                   Both give identical results.
  *   workspace       device scratch of at least rlic_workspace_bytes(...)
  *                   bytes, 256-byte aligned, or NULL to let the call allocate
  *                   it stream-ordered (cudaMallocAsync / cudaFreeAsync).
@@ -149,8 +165,14 @@ RLIC_API int rlic_trace_cells_f64(const double *u, const double *v, int64_t ny, 
  *   which reads u and v from two views (src/lib.rs:332-335).
  *
  * rlic_sweep_*: one convolution pass, `convolve` of src/lib.rs:364-406:
- *   tex_out = LIC(tex_in) along the packed field.  `flags` takes the
- *   variant bits only.
+ *   tex_out = LIC(tex_in) along the packed field.  When `codes` is not NULL
+ *   (rlic_path_code_bytes() bytes, 4-byte aligned) the pass also records
+ *   every streamline step there.  `flags` takes the variant bits only.
+ *
+ * rlic_replay_*: one convolution pass replayed from `codes` recorded by
+ *   rlic_sweep_* on the same ny x nx image with the same klen (boundaries
+ *   and uv mode are part of the record).  Identical results to
+ *   rlic_sweep_*; `flags` takes RLIC_FLAG_NO_FMA only.
  */
 RLIC_API int rlic_pack_field_f32(const float *u, const float *v, int64_t ny, int64_t nx,
                                  void *uv, void *stream);
@@ -159,11 +181,17 @@ RLIC_API int rlic_pack_field_f64(const double *u, const double *v, int64_t ny, i
 RLIC_API int rlic_sweep_f32(const float *tex_in, const void *uv, int64_t ny, int64_t nx,
                             const float *kernel, int64_t klen, int uv_mode, int bx_left,
                             int bx_right, int by_left, int by_right, float *tex_out,
-                            void *stream, unsigned flags);
+                            void *codes, void *stream, unsigned flags);
 RLIC_API int rlic_sweep_f64(const double *tex_in, const void *uv, int64_t ny, int64_t nx,
                             const double *kernel, int64_t klen, int uv_mode, int bx_left,
                             int bx_right, int by_left, int by_right, double *tex_out,
-                            void *stream, unsigned flags);
+                            void *codes, void *stream, unsigned flags);
+RLIC_API int rlic_replay_f32(const float *tex_in, const void *codes, int64_t ny, int64_t nx,
+                             const float *kernel, int64_t klen, float *tex_out, void *stream,
+                             unsigned flags);
+RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny, int64_t nx,
+                             const double *kernel, int64_t klen, double *tex_out,
+                             void *stream, unsigned flags);
 
 /*
  * Launch-shape tuning for the streamline kernels: CTA width and height in

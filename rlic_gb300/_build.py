@@ -42,7 +42,7 @@ NVCC_FLAGS = [
     "-warn-spills",
 ]
 
-SOURCES = ["lic_capi.cu"]
+SOURCES = ["lic_capi.cu", "lic_kernels_f32.cu", "lic_kernels_f64.cu"]
 
 
 def nvcc_path() -> str:
@@ -67,7 +67,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     """Compile every CUDA translation unit and link ``librlic_gb300.so``."""
     nvcc = nvcc_path()
     BUILD_DIR.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + [REPO_DIR / "include" / "rlic_gb300.h"]
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [
+        REPO_DIR / "include" / "rlic_gb300.h"
+    ]
     objs: list[Path] = []
     jobs: list[list[str]] = []
     for src in SOURCES:

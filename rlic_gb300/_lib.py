@@ -192,7 +192,7 @@ def _convolve_torch(
         out = torch.empty_like(tex_c, memory_format=torch.contiguous_format)
         ny, nx = tex_c.shape
         elem = tex_c.element_size()
-        nbytes = lib.rlic_workspace_bytes(ny, nx, k_c.shape[0], iterations, elem)
+        nbytes = lib.rlic_workspace_bytes(ny, nx, k_c.shape[0], iterations, elem, 0)
         ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
         stream = torch.cuda.current_stream(dev).cuda_stream
         fn = lib.rlic_convolve_f32 if tex_c.dtype == torch.float32 else lib.rlic_convolve_f64

@@ -26,6 +26,7 @@ RLIC_UV_POLARIZATION = 1
 RLIC_FLAG_HOST_MEMORY = 0x1
 RLIC_FLAG_NO_FMA = 0x2
 RLIC_FLAG_NO_BRANCHLESS = 0x4
+RLIC_FLAG_NO_PATH_CACHE = 0x8
 
 UV_MODE_CODES: dict[str, int] = {
     "velocity": RLIC_UV_VELOCITY,
@@ -44,17 +45,20 @@ _TRACE_ARGS = [_P, _P, _I64, _I64, _I64, _INT, _INT, _INT, _INT, _INT, _I64, _P,
 SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_version": ([], ctypes.c_char_p),
     "rlic_last_error": ([], ctypes.c_char_p),
-    "rlic_workspace_bytes": ([_I64, _I64, _I64, _I64, _INT], _SZ),
+    "rlic_workspace_bytes": ([_I64, _I64, _I64, _I64, _INT, _U], _SZ),
+    "rlic_path_code_bytes": ([_I64, _I64, _I64], _SZ),
     "rlic_convolve_f32": (_CONVOLVE_ARGS, _INT),
     "rlic_convolve_f64": (_CONVOLVE_ARGS, _INT),
     "rlic_trace_cells_f32": (_TRACE_ARGS, _INT),
     "rlic_trace_cells_f64": (_TRACE_ARGS, _INT),
     "rlic_pack_field_f32": ([_P, _P, _I64, _I64, _P, _P], _INT),
     "rlic_pack_field_f64": ([_P, _P, _I64, _I64, _P, _P], _INT),
-    "rlic_sweep_f32": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _U],
-                       _INT),
-    "rlic_sweep_f64": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _U],
-                       _INT),
+    "rlic_sweep_f32": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _P,
+                        _U], _INT),
+    "rlic_sweep_f64": ([_P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT, _P, _P, _P,
+                        _U], _INT),
+    "rlic_replay_f32": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
+    "rlic_replay_f64": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
 }

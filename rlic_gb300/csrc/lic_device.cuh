@@ -6,7 +6,7 @@
 //
 //   * products and sums that Rust rounds separately use the __*_rn
 //     intrinsics, which the compiler never contracts into an FMA;
-//   * Rust's `mul_add` is fma()/fmaf() (one rounding);
+//   * Rust's `mul_add` is __fmaf_rn / __fma_rn (one rounding);
 //   * divisions are __fdiv_rn / __ddiv_rn (IEEE round-to-nearest), never an
 //     approximate reciprocal;
 //   * the library is also built with -fmad=false -prec-div=true -ftz=false as
@@ -39,21 +39,73 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
 __device__ __forceinline__ double abs_(double a) { return fabs(a); }
 
-// num-traits Signed::signum for floats (std f32/f64::signum): -1 when the sign
-// bit is set (including -0.0 and -inf), +1 otherwise, NaN for NaN.
+// Accumulation of one kernel-weighted sample: `mul_add` in the default build
+// (src/lib.rs:357-360, 380-383), a rounded product then a rounded sum without
+// the `fma` feature (src/lib.rs:353-356, 376-379).
+template <typename T, bool FMA>
+__device__ __forceinline__ T accumulate(T w, T x, T acc) {
+    if constexpr (FMA) {
+        return fma_rn(w, x, acc);
+    } else {
+        return add_rn(acc, mul_rn(w, x));
+    }
+}
+
+// Which operands of the time divisions are routed around the division
+// sequence (see abs_quotient): 0 none, 1 zero numerators, 2 zero numerators
+// and zero denominators.  1 is the fastest on the at-scale workload (8192^2
+// float32): zero numerators are frequent (reversals), zero components rare,
+// and the full guard's extra selects cost more than the slow paths it saves.
+#ifndef RLIC_QUOTIENT_GUARD
+#define RLIC_QUOTIENT_GUARD 1
+#endif
+
+// |a / b| rounded to nearest, for b not NaN.  A zero numerator or a zero
+// denominator sends the division sequence to its slow path, and a warp whose
+// lanes take it runs it for all of them.  Such operands are common here: a
+// streamline that reverses direction meets a zero numerator every other
+// step, and axis-aligned flows have a zero velocity component at every step.
+// Their IEEE results are fixed, so they are produced by selects and the
+// division only sees fast-path operands:
+//   b == +-0:  a == +-0 or NaN -> NaN, otherwise inf
+//   a == +-0:  0 (b is not NaN)
 template <typename T>
-__device__ __forceinline__ T signum(T x) {
-    return isnan(x) ? x : (signbit(x) ? T(-1) : T(1));
+__device__ __forceinline__ T abs_quotient(T a, T b) {
+#if RLIC_QUOTIENT_GUARD == 0
+    return abs_(div_rn(a, b));
+#elif RLIC_QUOTIENT_GUARD == 1
+    const bool a0 = (a == T(0));
+    const T q = abs_(div_rn(a0 ? T(1) : a, b));
+    return a0 ? ((b == T(0)) ? T(NAN) : T(0)) : q;
+#else
+    const bool a0 = (a == T(0));
+    const bool a0n = !(a < T(0) || a > T(0));  // zero or NaN
+    const bool b0 = (b == T(0));
+    const T q = abs_(div_rn((a0 | b0) ? T(1) : a, b0 ? T(1) : b));
+    return b0 ? (a0n ? T(NAN) : T(INFINITY)) : (a0 ? T(0) : q);
+#endif
+}
+
+// Signed quotient a / b, for the branchy variant (b nonzero and not NaN).
+template <typename T>
+__device__ __forceinline__ T signed_quotient(T a, T b) {
+    const bool a0 = (a == T(0));
+    const T q = div_rn(a0 ? T(1) : a, b);
+    return a0 ? ((signbit(a) != signbit(b)) ? T(-0.0) : T(0.0)) : q;
 }
 
 // time_to_next_pixel, src/lib.rs:157-180.
 //   branchless + fma (default build):  |fma(1 + signum(v), 0.5 - f, f) / v|
 //   branchless, no fma:                |((1 + signum(v)) * (0.5 - f) + f) / v|
 //   branchy:  v > 0: (1 - f) / v;  v < 0: -(f / v);  else +inf
+// On the branchless path v is never NaN here (a NaN sample stops the trace
+// before any advance, src/lib.rs:336-338), so 1 + signum(v) is exactly 2 when
+// the sign bit of v is clear and exactly 0 when it is set (num-traits
+// signum: -0.0 -> -1).
 template <typename T, bool FMA, bool BRANCHLESS>
 __device__ __forceinline__ T time_to_next_pixel(T vel, T frac) {
     if constexpr (BRANCHLESS) {
-        const T s = add_rn(T(1), signum(vel));
+        const T s = signbit(vel) ? T(0) : T(2);
         const T d = sub_rn(T(0.5), frac);
         T rem;
         if constexpr (FMA) {
@@ -61,17 +113,18 @@ __device__ __forceinline__ T time_to_next_pixel(T vel, T frac) {
         } else {
             rem = add_rn(mul_rn(s, d), frac);
         }
-        return abs_(div_rn(rem, vel));
+        return abs_quotient(rem, vel);
     } else {
-        if (vel > T(0)) return div_rn(sub_rn(T(1), frac), vel);
-        if (vel < T(0)) return -div_rn(frac, vel);
+        if (vel > T(0)) return signed_quotient(sub_rn(T(1), frac), vel);
+        if (vel < T(0)) return -signed_quotient(frac, vel);
         return T(INFINITY);
     }
 }
 
 // One image axis with its two boundary rules (BoundaryPair, src/lib.rs:70-96),
 // pre-resolved: a coordinate that stepped to -1 becomes `lo_to`, one that
-// stepped to `size` becomes `hi_to` (closed: clamp; periodic: wrap).
+// stepped to `size` becomes `hi_to` (closed: clamp; periodic: wrap).  The
+// fraction is left alone, as in the reference.
 template <typename I>
 struct Axis {
     I size;
@@ -89,108 +142,235 @@ __host__ __device__ inline Axis<I> make_axis(I size, int left, int right) {
     return a;
 }
 
+// Image geometry of one launch.
 template <typename I>
-__device__ __forceinline__ I apply_axis(I c, const Axis<I>& a) {
-    c = (c == I(-1)) ? a.lo_to : c;
-    c = (c == a.size) ? a.hi_to : c;
-    return c;
+struct Geometry {
+    I ny, nx;
+    Axis<I> ax, ay;
+};
+
+// Step codes of the path cache: 4 bits per streamline step.
+//   0      no move (zero velocity, or a move cancelled by a closed boundary)
+//   1, 2   +1 / -1 column            3, 4   +1 / -1 row
+//   5, 6   wrap right -> left (-(nx-1)) / left -> right (+(nx-1))
+//   7, 8   wrap bottom -> top (-(ny-1) rows) / top -> bottom (+(ny-1) rows)
+//   15     the trace stopped on a NaN sample (this and all later steps)
+// The linear-index delta of each code is in the table below; replaying the
+// deltas from the start pixel visits exactly the cells the trace visited.
+constexpr uint32_t kStop = 15u;
+
+template <typename I>
+__device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
+    // called by one thread
+    for (int c = 0; c < 16; ++c) table[c] = 0;
+    table[1] = 1;
+    table[2] = -1;
+    table[3] = nx;
+    table[4] = -nx;
+    table[5] = -(nx - 1);
+    table[6] = nx - 1;
+    table[7] = -(ny - 1) * nx;
+    table[8] = (ny - 1) * nx;
 }
 
-// advance, src/lib.rs:236-273, with update_state (src/lib.rs:209-233) inlined.
-// (u, v) is the already sign-adjusted local velocity.  Ties and NaN times
-// take the y branch (`tx < ty` is false).  Both axes get the boundary rule
-// after every step (src/lib.rs:270-272); only the moved axis can be out of
-// range, and applying the rule to an in-range coordinate is the identity.
-template <typename T, bool FMA, bool BRANCHLESS, typename I>
-__device__ __forceinline__ void advance(T u, T v, I& i, I& j, T& fx, T& fy,
-                                        const Axis<I>& ax, const Axis<I>& ay) {
-    if (u == T(0) && v == T(0)) return;
-    const T tx = time_to_next_pixel<T, FMA, BRANCHLESS>(u, fx);
-    const T ty = time_to_next_pixel<T, FMA, BRANCHLESS>(v, fy);
+// advance, src/lib.rs:236-273, with update_state (src/lib.rs:209-233) folded
+// in, on one pixel state.  (u, v) is the sign-adjusted local velocity.
+//
+// Ties and NaN times take the y branch (`tx < ty` is false); -0.0 counts as
+// >= 0 (src/lib.rs:217).  A zero velocity leaves everything unchanged
+// (src/lib.rs:242-244); this is applied with selects rather than a branch so
+// that a warp whose lanes sit on zero cells stays converged.
+//
+// EDGE = false is the interior fast path: the caller guarantees no step can
+// reach the image border, so the boundary rule (src/lib.rs:270-272) is the
+// identity and only the linear index is tracked.  EDGE = true tracks the row
+// and column and applies the rule to the moved axis (the other axis is in
+// range already, and the rule is the identity on in-range coordinates).
+//
+// Returns the step code (see above).
+template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
+__device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
+                                            const Geometry<I>& g) {
+    const bool still = (u == T(0)) & (v == T(0));
+    // A still lane keeps its state whatever the times are; giving it unit
+    // velocities keeps its divisions on the fast path (a division by zero
+    // takes the slow one) and its lane in step with the warp.
+    const T su = still ? T(1) : u;
+    const T sv = still ? T(1) : v;
+    const T tx = time_to_next_pixel<T, FMA, BRANCHLESS>(su, fx);
+    const T ty = time_to_next_pixel<T, FMA, BRANCHLESS>(sv, fy);
     const bool xstep = tx < ty;
-    const T vpar = xstep ? u : v;
-    const T vorth = xstep ? v : u;
+    const T vpar = xstep ? su : sv;
+    const T vorth = xstep ? sv : su;
     const T t = xstep ? tx : ty;
-    T forth = xstep ? fy : fx;
+    const T forth_in = xstep ? fy : fx;
+    T forth;
     if constexpr (FMA) {
-        forth = fma_rn(t, vorth, forth);
+        forth = fma_rn(t, vorth, forth_in);
     } else {
-        forth = add_rn(forth, mul_rn(t, vorth));
+        forth = add_rn(forth_in, mul_rn(t, vorth));
     }
-    const bool up = vpar >= T(0);  // -0.0 counts as >= 0 (src/lib.rs:217)
+    const bool up = vpar >= T(0);
     const T fpar = up ? T(0) : T(1);
-    const I d = up ? I(1) : I(-1);
-    if (xstep) {
-        j = apply_axis(j + d, ax);
-        fx = fpar;
-        fy = forth;
+    const T nfx = xstep ? fpar : forth;
+    const T nfy = xstep ? forth : fpar;
+    fx = still ? fx : nfx;
+    fy = still ? fy : nfy;
+    if constexpr (!EDGE) {
+        const I step = xstep ? I(1) : g.nx;
+        cell += still ? I(0) : (up ? step : -step);
+        const uint32_t code = xstep ? (up ? 1u : 2u) : (up ? 3u : 4u);
+        return still ? 0u : code;
     } else {
-        i = apply_axis(i + d, ay);
-        fy = fpar;
-        fx = forth;
+        const I c_old = xstep ? j : i;
+        const I size = xstep ? g.ax.size : g.ay.size;
+        const I lo_to = xstep ? g.ax.lo_to : g.ay.lo_to;
+        const I hi_to = xstep ? g.ax.hi_to : g.ay.hi_to;
+        I c = c_old + (up ? I(1) : I(-1));
+        c = (c == I(-1)) ? lo_to : c;
+        c = (c == size) ? hi_to : c;
+        c = still ? c_old : c;
+        const I dd = c - c_old;
+        if (xstep) {
+            j = c;
+        } else {
+            i = c;
+        }
+        cell += xstep ? dd : dd * g.nx;
+        uint32_t code;
+        if (dd == I(0)) {
+            code = 0u;
+        } else if (dd == I(1)) {
+            code = xstep ? 1u : 3u;
+        } else if (dd == I(-1)) {
+            code = xstep ? 2u : 4u;
+        } else if (dd < I(0)) {
+            code = xstep ? 5u : 7u;
+        } else {
+            code = xstep ? 6u : 8u;
+        }
+        return code;
     }
 }
 
-// Read-only cached loads.
-template <typename V>
-__device__ __forceinline__ V ldg(const V* p) { return __ldg(p); }
+// Per-trace state of convole_single_pixel (src/lib.rs:314-323).
+template <typename T, typename I>
+struct TraceState {
+    T fx, fy;  // position inside the cell, starting at the centre (0.5, 0.5)
+    T lu, lv;  // previous sample in polarization mode, starting at (0, 0)
+    I cell, i, j;
+};
+
+// One step of convole_single_pixel (src/lib.rs:331-361): read u and v at the
+// current cell, stop on NaN (returns false), flip the sample against the
+// previous one in polarization mode (the dot product is two separately
+// rounded products and a rounded sum, src/lib.rs:341), negate it for the
+// backward trace, advance, then accumulate weight * texture at the new cell.
+// `code` receives the step code.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
+          bool SAMPLE, typename I>
+__device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
+                                           const Geometry<I>& g,
+                                           const typename Vec2<T>::type* __restrict__ uv,
+                                           const T* __restrict__ tex, uint32_t& code) {
+    const auto p = __ldg(uv + st.cell);
+    T pu = p.x, pv = p.y;
+    if (isnan(pu) || isnan(pv)) return false;
+    if constexpr (POL) {
+        const T dot = add_rn(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
+        if (dot < T(0)) {
+            pu = -pu;
+            pv = -pv;
+        }
+        st.lu = pu;
+        st.lv = pv;
+    }
+    if constexpr (BACKWARD) {
+        pu = -pu;
+        pv = -pv;
+    }
+    code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, g);
+    if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, __ldg(tex + st.cell), acc);
+    return true;
+}
 
 // One half of convole_single_pixel (src/lib.rs:305-362): the forward trace
 // (taps kmid+1 .. klen-1, ascending) or the backward trace (taps kmid-1 .. 0,
 // descending), accumulating kernel[k] * input[cell] into `acc` after each
-// step.  The reference reads u and v at the current cell, stops on NaN,
-// flips the sample against the previous one in polarization mode (the dot
-// product is two separately rounded products and a rounded sum,
-// src/lib.rs:341), negates it for the backward trace, advances, then samples
-// the texture at the new cell.
+// step.  `w` holds this half's weights in step order (w[s] is the tap of
+// step s), 8-entry aligned.  When SAMPLE is false the texture is not read.
 //
-// `Rec` receives (step, linear cell) after each step when RECORD is true.
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool RECORD,
-          typename I, typename Rec>
-__device__ __forceinline__ void trace_half(T& acc, I i, I j, I nx,
+// Steps run in groups of 8, one 32-bit word of step codes per group; with
+// RECORD the word is stored at words[group * stride].  A trace that stops on
+// NaN stores the stop code in place of its step and nothing after it.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
+          bool SAMPLE, bool RECORD, typename I>
+__device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
-                                           const T* __restrict__ tex,
-                                           const T* __restrict__ weights, int k0, int count,
-                                           const Axis<I>& ax, const Axis<I>& ay, Rec rec) {
-    T fx = T(0.5), fy = T(0.5);
-    T lu = T(0), lv = T(0);
-    for (int s = 0; s < count; ++s) {
-        const int k = BACKWARD ? k0 - s : k0 + s;
-        const auto p = ldg(uv + (i * nx + j));
-        T pu = p.x, pv = p.y;
-        if (isnan(pu) || isnan(pv)) break;
-        if constexpr (POL) {
-            const T dot = add_rn(mul_rn(pu, lu), mul_rn(pv, lv));
-            if (dot < T(0)) {
-                pu = -pu;
-                pv = -pv;
+                                           const T* __restrict__ tex, const T* w, int count,
+                                           uint32_t* __restrict__ words, size_t stride) {
+    TraceState<T, I> st;
+    st.fx = T(0.5);
+    st.fy = T(0.5);
+    st.lu = T(0);
+    st.lv = T(0);
+    st.cell = i * g.nx + j;
+    st.i = i;
+    st.j = j;
+    const int full = count >> 3;
+    for (int q = 0; q < full; ++q) {
+        const T* wq = w + 8 * q;
+        uint32_t word = 0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            uint32_t code = 0;
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE>(
+                    st, acc, SAMPLE ? wq[b] : T(0), g, uv, tex, code)) {
+                if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
+                return;
             }
-            lu = pu;
-            lv = pv;
+            word |= code << (4 * b);
         }
-        if constexpr (BACKWARD) {
-            pu = -pu;
-            pv = -pv;
-        }
-        advance<T, FMA, BRANCHLESS>(pu, pv, i, j, fx, fy, ax, ay);
-        const I cell = i * nx + j;
-        if constexpr (RECORD) {
-            rec(s, cell);
-        } else {
-            const T x = ldg(tex + cell);
-            const T w = weights[k];
-            if constexpr (FMA) {
-                acc = fma_rn(w, x, acc);
-            } else {
-                acc = add_rn(acc, mul_rn(w, x));
+        if constexpr (RECORD) words[size_t(q) * stride] = word;
+    }
+    const int rest = count & 7;
+    if (rest) {
+        uint32_t word = 0;
+        for (int b = 0; b < rest; ++b) {
+            uint32_t code = 0;
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE>(
+                    st, acc, SAMPLE ? w[8 * full + b] : T(0), g, uv, tex, code)) {
+                if constexpr (RECORD) words[size_t(full) * stride] = word | (kStop << (4 * b));
+                return;
             }
+            word |= code << (4 * b);
         }
+        if constexpr (RECORD) words[size_t(full) * stride] = word;
     }
 }
 
-struct NoRecord {
-    template <typename I>
-    __device__ __forceinline__ void operator()(int, I) const {}
-};
+// The same walk for path parity checks: reports the cell reached by every
+// step to `rec(s, cell)`.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, typename I, typename Rec>
+__device__ __forceinline__ void walk_half(I i, I j, const Geometry<I>& g,
+                                          const typename Vec2<T>::type* __restrict__ uv,
+                                          int count, Rec rec) {
+    TraceState<T, I> st;
+    st.fx = T(0.5);
+    st.fy = T(0.5);
+    st.lu = T(0);
+    st.lv = T(0);
+    st.cell = i * g.nx + j;
+    st.i = i;
+    st.j = j;
+    T acc = T(0);
+    for (int s = 0; s < count; ++s) {
+        uint32_t code = 0;
+        if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, true, false>(
+                st, acc, T(0), g, uv, static_cast<const T*>(nullptr), code))
+            return;
+        rec(s, st.cell);
+    }
+}
 
 }  // namespace rlic

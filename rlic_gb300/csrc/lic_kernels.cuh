@@ -1,0 +1,442 @@
+// lic_kernels.cuh -- CUDA kernels of the convolution core and their launchers.
+//
+// Included by exactly one translation unit per element type
+// (lic_kernels_f32.cu, lic_kernels_f64.cu), which instantiate the launchers
+// declared in lic_launch.h.
+//
+// Kernels
+//   pack_uv_kernel     u, v -> interleaved (u, v) pairs (one load per step)
+//   lic_pass_kernel    one convolution pass (src/lib.rs:364-406): one thread
+//                      per pixel, centre tap, forward trace, backward trace;
+//                      optionally records every step's code (path cache)
+//   lic_gather_kernel  one convolution pass replayed from recorded step codes:
+//                      the same cells, weights and accumulation order as the
+//                      traced pass, without re-running the streamline
+//                      arithmetic (the path of a pixel does not depend on the
+//                      texture, src/lib.rs:433-440 reuses u, v every pass)
+//   trace_cells_kernel streamline cells of selected pixels (parity checks)
+//
+// Work distribution: CTAs of block_x x block_y threads own pixel tiles of the
+// same shape, numbered row-major.  The traced pass launches one CTA per tile
+// (tiles cost unevenly, and the hardware scheduler balances them); the
+// replay, whose tiles all cost the same, sizes its grid to the CTAs that fit
+// on the device at once and strides over tiles, so its shared-memory set-up
+// (weights, delta table) happens once per CTA.  A tile whose streamlines
+// cannot reach the border (every pixel farther than klen/2 cells from it)
+// takes the interior path without boundary logic.
+#pragma once
+
+#include "lic_device.cuh"
+#include "lic_launch.h"
+
+// Minimum resident CTAs per SM requested from the register allocator for the
+// float32 traced pass (256-thread CTAs; 8 = full occupancy at 32
+// registers/thread).  The float64 pass needs more registers and keeps 1.
+#ifndef RLIC_PASS_MIN_BLOCKS_F32
+#define RLIC_PASS_MIN_BLOCKS_F32 1
+#endif
+
+namespace rlic {
+
+template <typename T> struct PassMinBlocks { static constexpr int value = 1; };
+template <> struct PassMinBlocks<float> { static constexpr int value = RLIC_PASS_MIN_BLOCKS_F32; };
+
+template <typename T>
+__global__ void pack_uv_kernel(const T* __restrict__ u, const T* __restrict__ v,
+                               typename Vec2<T>::type* __restrict__ uv, int64_t n) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        typename Vec2<T>::type p;
+        p.x = u[k];
+        p.y = v[k];
+        uv[k] = p;
+    }
+}
+
+// Tile bookkeeping shared by the pass and gather kernels.
+template <typename I>
+struct TileGrid {
+    I tiles_x, ntiles;
+    int bx, by;
+    int radius;  // max cells a streamline can move away from its pixel
+};
+
+template <typename I>
+__device__ __forceinline__ bool tile_is_interior(I ti, I tj, const TileGrid<I>& tg,
+                                                 const Geometry<I>& g) {
+    const I r0 = ti * tg.by, c0 = tj * tg.bx;
+    const I r = tg.radius;
+    return r0 - r >= 0 && r0 + tg.by - 1 + r <= g.ny - 1 && c0 - r >= 0 &&
+           c0 + tg.bx - 1 + r <= g.nx - 1;
+}
+
+// Shared-memory layout: forward weights in step order (wf[s] = kernel[kmid+1+s]),
+// then backward weights in step order (wb[s] = kernel[kmid-1-s]), each padded
+// to a multiple of 8 entries; then (gather only) the 16-entry delta table.
+template <typename T>
+__device__ __forceinline__ void load_step_weights(T* smem, const T* __restrict__ kernel, int klen,
+                                                  int nf_pad) {
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nthreads = blockDim.x * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int s = tid; s < nf; s += nthreads) smem[s] = kernel[kmid + 1 + s];
+    for (int s = tid; s < kmid; s += nthreads) smem[nf_pad + s] = kernel[kmid - 1 - s];
+}
+
+// Path-cache word addressing: codes[word * npix + pixel], 8 steps per word,
+// forward words first, then backward words (word-major so that a warp's
+// 32 consecutive pixels read or write 128 contiguous bytes).
+struct CodeLayout {
+    int64_t npix;
+    int words_f;  // ceil(nf / 8)
+};
+
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, bool RECORD, typename I>
+__device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
+                                            const typename Vec2<T>::type* __restrict__ uv,
+                                            const T* __restrict__ tex, const T* wf, const T* wb,
+                                            T wmid, int nf, int kmid, uint32_t* __restrict__ codes,
+                                            const CodeLayout& cl) {
+    const I p = i * g.nx + j;
+    T acc = accumulate<T, FMA>(wmid, __ldg(tex + p), T(0));
+    uint32_t* words_f = RECORD ? codes + p : nullptr;
+    uint32_t* words_b = RECORD ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : nullptr;
+    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, true, RECORD>(acc, i, j, g, uv, tex, wf,
+                                                                   nf, words_f, cl.npix);
+    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, true, RECORD>(acc, i, j, g, uv, tex, wb,
+                                                                  kmid, words_b, cl.npix);
+    return acc;
+}
+
+// One convolution pass, one pixel tile per CTA (the hardware balances CTAs of
+// uneven cost, e.g. streamlines that stop early).
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool RECORD, typename I>
+__global__ void __launch_bounds__(256, PassMinBlocks<T>::value)
+lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __restrict__ uv,
+                const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
+                T* __restrict__ tex_out, uint32_t* __restrict__ codes, CodeLayout cl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* wsm = reinterpret_cast<T*>(smem_raw);
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nf_pad = (nf + 7) & ~7;
+    load_step_weights(wsm, kernel, klen, nf_pad);
+    __syncthreads();
+    const T wmid = __ldg(kernel + kmid);
+    const I tile = I(blockIdx.x);
+    const I ti = tile / tg.tiles_x;
+    const I tj = tile - ti * tg.tiles_x;
+    const I i = ti * tg.by + I(threadIdx.y);
+    const I j = tj * tg.bx + I(threadIdx.x);
+    if (tile_is_interior(ti, tj, tg, g)) {
+        tex_out[i * g.nx + j] = convolve_pixel<T, FMA, BRANCHLESS, POL, false, RECORD>(
+            i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+    } else if (i < g.ny && j < g.nx) {
+        tex_out[i * g.nx + j] = convolve_pixel<T, FMA, BRANCHLESS, POL, true, RECORD>(
+            i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+    }
+}
+
+// True when one of the 8 codes of a word is the stop code (all four bits set).
+__device__ __forceinline__ bool word_has_stop(uint32_t wd) {
+    return (wd & (wd >> 1) & (wd >> 2) & (wd >> 3) & 0x11111111u) != 0u;
+}
+
+// Replays `count` recorded steps of one half from pixel p.  Words without a
+// stop code (all of them unless the field holds NaNs) run branch-free: the 8
+// deltas, the 8 cells and the 8 texture loads are independent of the
+// accumulation, so they are all in flight before the 8 ordered FMAs.
+template <typename T, bool FMA, typename I>
+__device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restrict__ words,
+                                            int64_t npix, int count, const T* w, const I* table,
+                                            const T* __restrict__ tex) {
+    I cell = p;
+    const int full = count >> 3;
+    for (int q = 0; q <= full; ++q) {
+        const int n = (q < full) ? 8 : (count & 7);
+        if (n == 0) break;
+        const uint32_t wd = __ldg(words + size_t(q) * size_t(npix));
+        const T* wq = w + 8 * q;
+        if (n == 8 && !word_has_stop(wd)) {
+            T x[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                cell += table[(wd >> (4 * b)) & 15u];
+                x[b] = __ldg(tex + cell);
+            }
+#pragma unroll
+            for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
+        } else {
+            for (int b = 0; b < n; ++b) {
+                const uint32_t code = (wd >> (4 * b)) & 15u;
+                if (code == kStop) return;
+                cell += table[code];
+                acc = accumulate<T, FMA>(wq[b], __ldg(tex + cell), acc);
+            }
+        }
+    }
+}
+
+template <typename T, bool FMA, typename I>
+__global__ void __launch_bounds__(256)
+lic_gather_kernel(const T* __restrict__ tex_in, const uint32_t* __restrict__ codes,
+                  const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
+                  T* __restrict__ tex_out, CodeLayout cl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* wsm = reinterpret_cast<T*>(smem_raw);
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nf_pad = (nf + 7) & ~7;
+    const int nb_pad = (kmid + 7) & ~7;
+    I* table = reinterpret_cast<I*>(smem_raw + sizeof(T) * size_t(nf_pad + nb_pad));
+    load_step_weights(wsm, kernel, klen, nf_pad);
+    if (threadIdx.x == 0 && threadIdx.y == 0) fill_delta_table(table, g.nx, g.ny);
+    __syncthreads();
+    const T wmid = __ldg(kernel + kmid);
+    const uint32_t* codes_b = codes + size_t(cl.words_f) * size_t(cl.npix);
+    for (I tile = blockIdx.x; tile < tg.ntiles; tile += gridDim.x) {
+        const I ti = tile / tg.tiles_x;
+        const I tj = tile - ti * tg.tiles_x;
+        const I i = ti * tg.by + I(threadIdx.y);
+        const I j = tj * tg.bx + I(threadIdx.x);
+        if (i >= g.ny || j >= g.nx) continue;
+        const I p = i * g.nx + j;
+        T acc = accumulate<T, FMA>(wmid, __ldg(tex_in + p), T(0));
+        replay_half<T, FMA, I>(acc, p, codes + p, cl.npix, nf, wsm, table, tex_in);
+        replay_half<T, FMA, I>(acc, p, codes_b + p, cl.npix, kmid, wsm + nf_pad, table, tex_in);
+        tex_out[p] = acc;
+    }
+}
+
+// Cells visited by the streamlines of selected pixels (path parity checks).
+template <typename T, bool FMA, bool BRANCHLESS, bool POL>
+__global__ void trace_cells_kernel(const typename Vec2<T>::type* __restrict__ uv,
+                                   Geometry<int64_t> g, int klen, int64_t npix,
+                                   const int64_t* __restrict__ pix, int64_t* __restrict__ cells) {
+    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const int steps = klen - 1;
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    int64_t* dst = cells + p * steps;
+    for (int s = 0; s < steps; ++s) dst[s] = -1;
+    const int64_t lin = pix[p];
+    if (lin < 0 || lin >= g.ny * g.nx) return;  // invalid pixel: row stays -1
+    const int64_t i = lin / g.nx;
+    const int64_t j = lin - i * g.nx;
+    walk_half<T, FMA, BRANCHLESS, POL, false>(i, j, g, uv, nf,
+                                              [dst](int s, int64_t c) { dst[s] = c; });
+    walk_half<T, FMA, BRANCHLESS, POL, true>(i, j, g, uv, kmid,
+                                             [dst, nf](int s, int64_t c) { dst[nf + s] = c; });
+}
+
+// ---------------------------------------------------------------- launchers --
+
+inline int64_t tiles_of(int64_t n, int b) { return (n + b - 1) / b; }
+
+template <typename I>
+Geometry<I> make_geometry(const Shape& sh) {
+    Geometry<I> g;
+    g.ny = I(sh.ny);
+    g.nx = I(sh.nx);
+    g.ax = make_axis<I>(I(sh.nx), sh.bnd[0], sh.bnd[1]);
+    g.ay = make_axis<I>(I(sh.ny), sh.bnd[2], sh.bnd[3]);
+    return g;
+}
+
+template <typename I>
+TileGrid<I> make_tiles(const Shape& sh, const LaunchConfig& lc, int klen) {
+    TileGrid<I> tg;
+    tg.bx = lc.block_x;
+    tg.by = lc.block_y;
+    tg.tiles_x = I(tiles_of(sh.nx, lc.block_x));
+    tg.ntiles = tg.tiles_x * I(tiles_of(sh.ny, lc.block_y));
+    tg.radius = klen / 2;
+    return tg;
+}
+
+inline CodeLayout make_code_layout(const Shape& sh, int klen) {
+    CodeLayout cl;
+    cl.npix = sh.ny * sh.nx;
+    const int nf = klen - klen / 2 - 1;
+    cl.words_f = (nf + 7) / 8;
+    return cl;
+}
+
+inline size_t weights_smem_bytes(int klen, size_t elem) {
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    return elem * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7));
+}
+
+// Grid size for a persistent-stride kernel: CTAs resident at once, capped by
+// the number of tiles.
+template <typename K>
+cudaError_t persistent_grid(K kernel, int threads, size_t smem, int64_t ntiles,
+                            unsigned* grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int64_t g = int64_t(sms) * per_sm;
+    if (g > ntiles) g = ntiles;
+    if (g < 1) g = 1;
+    *grid = unsigned(g);
+    return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t launch_pack_t(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) {
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    pack_uv_kernel<T><<<unsigned(blocks), 256, 0, stream>>>(
+        u, v, static_cast<typename Vec2<T>::type*>(uv), n);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool RECORD, typename I>
+cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int klen,
+                          const Shape& sh, const LaunchConfig& lc, T* tex_out, uint32_t* codes,
+                          cudaStream_t stream) {
+    const auto g = make_geometry<I>(sh);
+    const auto tg = make_tiles<I>(sh, lc, klen);
+    const auto cl = make_code_layout(sh, klen);
+    const size_t smem = weights_smem_bytes(klen, sizeof(T));
+    if (int64_t(tg.ntiles) > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    auto kfn = lic_pass_kernel<T, FMA, BRANCHLESS, POL, RECORD, I>;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    kfn<<<unsigned(tg.ntiles), dim3(lc.block_x, lc.block_y), smem, stream>>>(
+        tex_in, static_cast<const typename Vec2<T>::type*>(uv), kernel, klen, g, tg, tex_out,
+        codes, cl);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, typename I>
+cudaError_t launch_pass_i(const Variant& var, bool record, const T* tex_in, const void* uv,
+                          const T* kernel, int klen, const Shape& sh, const LaunchConfig& lc,
+                          T* tex_out, uint32_t* codes, cudaStream_t stream) {
+    const int code = (var.fma ? 8 : 0) | (var.branchless ? 4 : 0) | (var.pol ? 2 : 0) |
+                     (record ? 1 : 0);
+#define RLIC_PASS_CASE(C, F, B, P, R)                                                      \
+    case C:                                                                                \
+        return launch_pass_t<T, F, B, P, R, I>(tex_in, uv, kernel, klen, sh, lc, tex_out,  \
+                                               codes, stream);
+    switch (code) {
+        RLIC_PASS_CASE(0, false, false, false, false)
+        RLIC_PASS_CASE(1, false, false, false, true)
+        RLIC_PASS_CASE(2, false, false, true, false)
+        RLIC_PASS_CASE(3, false, false, true, true)
+        RLIC_PASS_CASE(4, false, true, false, false)
+        RLIC_PASS_CASE(5, false, true, false, true)
+        RLIC_PASS_CASE(6, false, true, true, false)
+        RLIC_PASS_CASE(7, false, true, true, true)
+        RLIC_PASS_CASE(8, true, false, false, false)
+        RLIC_PASS_CASE(9, true, false, false, true)
+        RLIC_PASS_CASE(10, true, false, true, false)
+        RLIC_PASS_CASE(11, true, false, true, true)
+        RLIC_PASS_CASE(12, true, true, false, false)
+        RLIC_PASS_CASE(13, true, true, false, true)
+        RLIC_PASS_CASE(14, true, true, true, false)
+        RLIC_PASS_CASE(15, true, true, true, true)
+    }
+#undef RLIC_PASS_CASE
+    return cudaErrorInvalidValue;
+}
+
+template <typename T, bool FMA, typename I>
+cudaError_t launch_gather_t(const T* tex_in, const uint32_t* codes, const T* kernel, int klen,
+                            const Shape& sh, const LaunchConfig& lc, T* tex_out,
+                            cudaStream_t stream) {
+    const auto g = make_geometry<I>(sh);
+    const auto tg = make_tiles<I>(sh, lc, klen);
+    const auto cl = make_code_layout(sh, klen);
+    const size_t smem = weights_smem_bytes(klen, sizeof(T)) + 16 * sizeof(I);
+    auto kfn = lic_gather_kernel<T, FMA, I>;
+    unsigned grid = 0;
+    cudaError_t e = persistent_grid(kfn, lc.block_x * lc.block_y, smem, int64_t(tg.ntiles), &grid);
+    if (e != cudaSuccess) return e;
+    kfn<<<grid, dim3(lc.block_x, lc.block_y), smem, stream>>>(tex_in, codes, kernel, klen, g, tg,
+                                                              tex_out, cl);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_trace_cells_t(const Variant& var, const void* uv, const Shape& sh, int klen,
+                                 int64_t npix, const int64_t* pix, int64_t* cells,
+                                 cudaStream_t stream) {
+    const auto g = make_geometry<int64_t>(sh);
+    const auto* p = static_cast<const typename Vec2<T>::type*>(uv);
+    const unsigned blocks = unsigned((npix + 127) / 128);
+    const int code = (var.fma ? 4 : 0) | (var.branchless ? 2 : 0) | (var.pol ? 1 : 0);
+#define RLIC_TRACE_CASE(C, F, B, P)                                                       \
+    case C:                                                                               \
+        trace_cells_kernel<T, F, B, P><<<blocks, 128, 0, stream>>>(p, g, klen, npix, pix, \
+                                                                   cells);                \
+        break;
+    switch (code) {
+        RLIC_TRACE_CASE(0, false, false, false)
+        RLIC_TRACE_CASE(1, false, false, true)
+        RLIC_TRACE_CASE(2, false, true, false)
+        RLIC_TRACE_CASE(3, false, true, true)
+        RLIC_TRACE_CASE(4, true, false, false)
+        RLIC_TRACE_CASE(5, true, false, true)
+        RLIC_TRACE_CASE(6, true, true, false)
+        RLIC_TRACE_CASE(7, true, true, true)
+    }
+#undef RLIC_TRACE_CASE
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Definitions of the per-type overloads declared in lic_launch.h.
+#define RLIC_DEFINE_LAUNCHERS(T)                                                             \
+    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) { \
+        return launch_pack_t<T>(u, v, uv, n, stream);                                        \
+    }                                                                                        \
+    cudaError_t launch_pass(const Variant& var, bool record, const T* tex_in, const void* uv, \
+                            const T* kernel, int klen, const Shape& sh,                      \
+                            const LaunchConfig& lc, T* tex_out, uint32_t* codes,             \
+                            cudaStream_t stream) {                                           \
+        if (sh.small_index())                                                                \
+            return launch_pass_i<T, int32_t>(var, record, tex_in, uv, kernel, klen, sh, lc,  \
+                                             tex_out, codes, stream);                        \
+        return launch_pass_i<T, int64_t>(var, record, tex_in, uv, kernel, klen, sh, lc,      \
+                                         tex_out, codes, stream);                            \
+    }                                                                                        \
+    cudaError_t launch_gather(bool fma, const T* tex_in, const uint32_t* codes,              \
+                              const T* kernel, int klen, const Shape& sh,                    \
+                              const LaunchConfig& lc, T* tex_out, cudaStream_t stream) {     \
+        if (sh.small_index())                                                                \
+            return fma ? launch_gather_t<T, true, int32_t>(tex_in, codes, kernel, klen, sh,  \
+                                                           lc, tex_out, stream)              \
+                       : launch_gather_t<T, false, int32_t>(tex_in, codes, kernel, klen, sh, \
+                                                            lc, tex_out, stream);            \
+        return fma ? launch_gather_t<T, true, int64_t>(tex_in, codes, kernel, klen, sh, lc,  \
+                                                       tex_out, stream)                      \
+                   : launch_gather_t<T, false, int64_t>(tex_in, codes, kernel, klen, sh, lc, \
+                                                        tex_out, stream);                    \
+    }                                                                                        \
+    cudaError_t launch_trace_cells(const Variant& var, const T* /*type tag*/, const void* uv, \
+                                   const Shape& sh, int klen, int64_t npix,                  \
+                                   const int64_t* pix, int64_t* cells, cudaStream_t stream) { \
+        return launch_trace_cells_t<T>(var, uv, sh, klen, npix, pix, cells, stream);         \
+    }
+
+}  // namespace rlic

@@ -1,0 +1,63 @@
+// lic_launch.h -- host-side interface between the C ABI and the kernels.
+//
+// One overload of each launcher per element type (float, double), defined in
+// lic_kernels_f32.cu and lic_kernels_f64.cu.  All launchers are asynchronous
+// on `stream` and return the launch status.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rlic {
+
+// Arithmetic variant: the reference's Cargo features (Cargo.toml:27-30) and
+// the uv mode.
+struct Variant {
+    bool fma;
+    bool branchless;
+    bool pol;
+};
+
+// Image shape and boundary codes (x_left, x_right, y_left, y_right; 0 closed,
+// 1 periodic).
+struct Shape {
+    int64_t ny, nx;
+    int bnd[4];
+    bool small_index() const { return ny * nx < (int64_t(1) << 31) - 1; }
+};
+
+// CTA shape in pixels.
+struct LaunchConfig {
+    int block_x, block_y;
+};
+
+// Counts one kernel launch (rlic_kernel_launch_count).
+void count_launch();
+
+// 32-bit words of step codes per pixel for a kernel of klen taps (8 steps of
+// 4 bits per word, forward and backward halves padded separately).
+inline int64_t code_words_per_pixel(int64_t klen) {
+    const int64_t kmid = klen / 2;
+    const int64_t nf = klen - kmid - 1;
+    return (nf + 7) / 8 + (kmid + 7) / 8;
+}
+
+#define RLIC_DECLARE_LAUNCHERS(T)                                                          \
+    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream); \
+    cudaError_t launch_pass(const Variant& var, bool record, const T* tex_in, const void* uv, \
+                            const T* kernel, int klen, const Shape& sh,                    \
+                            const LaunchConfig& lc, T* tex_out, uint32_t* codes,           \
+                            cudaStream_t stream);                                          \
+    cudaError_t launch_gather(bool fma, const T* tex_in, const uint32_t* codes,            \
+                              const T* kernel, int klen, const Shape& sh,                  \
+                              const LaunchConfig& lc, T* tex_out, cudaStream_t stream);    \
+    cudaError_t launch_trace_cells(const Variant& var, const T* type_tag, const void* uv,  \
+                                   const Shape& sh, int klen, int64_t npix,                \
+                                   const int64_t* pix, int64_t* cells, cudaStream_t stream);
+
+RLIC_DECLARE_LAUNCHERS(float)
+RLIC_DECLARE_LAUNCHERS(double)
+
+#undef RLIC_DECLARE_LAUNCHERS
+
+}  // namespace rlic

@@ -34,12 +34,25 @@ def test_version(native) -> None:
 
 def test_workspace_bytes(native) -> None:
     ws = native.rlic_workspace_bytes
-    # packed (u, v) + kernel copy; + ping-pong buffer from two iterations on
-    assert ws(8192, 8192, 65, 1, 4) == 2 * 8192 * 8192 * 4 + 512
-    assert ws(8192, 8192, 65, 5, 4) == 3 * 8192 * 8192 * 4 + 512
-    assert ws(10, 10, 3, 2, 8) == 1792 + 1024 + 256
-    assert ws(0, 10, 3, 1, 4) == 0
-    assert ws(10, 10, 3, 1, 2) == 0
+    n = 8192 * 8192
+    # one pass: packed (u, v) + kernel copy
+    assert ws(8192, 8192, 65, 1, 4, 0) == 2 * n * 4 + 512
+    # five passes: + ping-pong buffer + path cache (8 words of 8 steps per pixel)
+    assert ws(8192, 8192, 65, 5, 4, 0) == 3 * n * 4 + 8 * 4 * n + 512
+    assert ws(8192, 8192, 65, 5, 4, 0x8) == 3 * n * 4 + 512
+    assert ws(10, 10, 3, 2, 8, 0) == 1792 + 1024 + 1024 + 256
+    assert ws(10, 10, 3, 2, 8, 0x8) == 1792 + 1024 + 256
+    assert ws(0, 10, 3, 1, 4, 0) == 0
+    assert ws(10, 10, 3, 1, 2, 0) == 0
+
+
+def test_path_code_bytes(native) -> None:
+    pc = native.rlic_path_code_bytes
+    assert pc(8192, 8192, 65) == 8 * 4 * 8192 * 8192  # 32 + 32 steps
+    assert pc(10, 10, 129) == 16 * 4 * 100  # 64 + 64 steps
+    assert pc(10, 10, 2) == 1 * 4 * 100  # 0 forward + 1 backward step
+    assert pc(10, 10, 18) == (1 + 2) * 4 * 100  # 8 forward + 9 backward steps
+    assert pc(0, 10, 3) == 0
 
 
 def _call(native, **over):
@@ -60,6 +73,7 @@ def _call(native, **over):
         (dict(iterations=-1), "iterations"),
         (dict(texture=None), "null"),
         (dict(flags=0x100), "flag"),
+        (dict(klen=1 << 21), "too long"),
     ],
 )
 def test_argument_errors(native, over, text) -> None:
@@ -76,6 +90,18 @@ def test_check_raises(native) -> None:
 
 def test_trace_argument_errors(native) -> None:
     rc = native.rlic_trace_cells_f64(1, 1, 4, 4, 3, 0, 0, 0, 0, 0, -1, 1, 1, None, 0)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+
+
+def test_sweep_and_replay_argument_errors(native) -> None:
+    # host-memory flag is not accepted by the device-only building blocks
+    rc = native.rlic_sweep_f32(1, 1, 4, 4, 1, 3, 0, 0, 0, 0, 0, 1, None, None, 0x1)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    rc = native.rlic_replay_f32(1, 1, 4, 4, 1, 3, 1, None, 0x4)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    rc = native.rlic_replay_f64(1, None, 4, 4, 1, 3, 1, None, 0)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    rc = native.rlic_pack_field_f32(1, 1, 4, 4, 3, None)  # misaligned pair array
     assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
 
 

@@ -50,7 +50,7 @@ def _variant_flags(variant: int) -> int:
 
 
 def capi_convolve(tex, u, v, k, uv_mode="velocity", boundaries="closed", iterations=1,
-                  variant=3):
+                  variant=3, extra_flags=0):
     """rlic_convolve_* with host buffers (the call copies in and out)."""
     lib = _native.lib()
     dtype = np.asarray(tex).dtype
@@ -60,7 +60,7 @@ def capi_convolve(tex, u, v, k, uv_mode="velocity", boundaries="closed", iterati
     ny, nx = tex.shape
     rc = fn(tex.ctypes.data, u.ctypes.data, v.ctypes.data, ny, nx, k.ctypes.data, k.size,
             int(uv_mode == "polarization"), *_codes(boundaries), iterations, out.ctypes.data,
-            None, 0, None, _native.RLIC_FLAG_HOST_MEMORY | _variant_flags(variant))
+            None, 0, None, _native.RLIC_FLAG_HOST_MEMORY | _variant_flags(variant) | extra_flags)
     _native.check(rc)
     return out
 
@@ -163,9 +163,12 @@ def test_random_fields(oracle, dtype, uv_mode, bnd, kind) -> None:
     u, v = _field(rng, ny, nx, dtype, kind)
     tex = rng.random((ny, nx)).astype(dtype)
     k = rng.random(31).astype(dtype)
-    want = oracle.convolve(tex, u, v, k, uv_mode=uv_mode, boundaries=bnd, iterations=2)
-    got = capi_convolve(tex, u, v, k, uv_mode, bnd, iterations=2)
+    want = oracle.convolve(tex, u, v, k, uv_mode=uv_mode, boundaries=bnd, iterations=3)
+    got = capi_convolve(tex, u, v, k, uv_mode, bnd, iterations=3)  # path cache
     assert_bitwise(got, want)
+    plain = capi_convolve(tex, u, v, k, uv_mode, bnd, iterations=3,
+                          extra_flags=_native.RLIC_FLAG_NO_PATH_CACHE)
+    assert_bitwise(plain, want)
     pix = np.arange(ny * nx)
     np.testing.assert_array_equal(
         capi_cells(u, v, 31, pix, uv_mode, bnd),
@@ -185,6 +188,9 @@ def test_feature_variants(oracle, variant, dtype) -> None:
                                iterations=2, variant=variant)
         got = capi_convolve(tex, u, v, k, mode, "periodic", 2, variant)
         assert_bitwise(got, want)
+        plain = capi_convolve(tex, u, v, k, mode, "periodic", 2, variant,
+                              _native.RLIC_FLAG_NO_PATH_CACHE)
+        assert_bitwise(plain, want)
 
 
 @pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (2, 2), (3, 130), (130, 3)])
@@ -198,6 +204,9 @@ def test_degenerate_shapes_and_kernels(oracle, shape, klen) -> None:
         want = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries=bnd, iterations=3)
         got = capi_convolve(tex, u, v, k, mode, bnd, iterations=3)
         assert_bitwise(got, want)
+        plain = capi_convolve(tex, u, v, k, mode, bnd, iterations=3,
+                              extra_flags=_native.RLIC_FLAG_NO_PATH_CACHE)
+        assert_bitwise(plain, want)
 
 
 @pytest.mark.parametrize("iterations", [0, 1, 2, 3, 4])
@@ -296,7 +305,7 @@ def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
     rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
-    assert _native.launch_count() - before == 4  # pack + 3 passes
+    assert _native.launch_count() - before == 4  # pack + traced pass + 2 replays
 
 
 def test_device_entry_points_with_workspace(oracle) -> None:
@@ -314,7 +323,7 @@ def test_device_entry_points_with_workspace(oracle) -> None:
                             iterations=3)
     d = {n: torch.from_numpy(a).cuda() for n, a in dict(t=tex, u=u, v=v, k=k).items()}
     out = torch.empty_like(d["t"])
-    nbytes = lib.rlic_workspace_bytes(70, 90, 33, 3, 4)
+    nbytes = lib.rlic_workspace_bytes(70, 90, 33, 3, 4, 0)
     ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     _native.check(lib.rlic_convolve_f32(
@@ -328,7 +337,21 @@ def test_device_entry_points_with_workspace(oracle) -> None:
     uv = torch.empty((70, 90, 2), dtype=torch.float32, device="cuda")
     _native.check(lib.rlic_pack_field_f32(d["u"].data_ptr(), d["v"].data_ptr(), 70, 90,
                                           uv.data_ptr(), stream))
+    codes = torch.empty(lib.rlic_path_code_bytes(70, 90, 33) // 4, dtype=torch.int32,
+                        device="cuda")
     _native.check(lib.rlic_sweep_f32(d["t"].data_ptr(), uv.data_ptr(), 70, 90,
                                      d["k"].data_ptr(), 33, 1, 1, 1, 1, 1, out.data_ptr(),
-                                     stream, 0))
+                                     codes.data_ptr(), stream, 0))
     assert_bitwise(out.cpu().numpy(), want1)
+    # replaying the recorded paths on another texture = tracing it
+    tex2 = torch.from_numpy(rng.random((70, 90)).astype(np.float32)).cuda()
+    traced = torch.empty_like(out)
+    _native.check(lib.rlic_sweep_f32(tex2.data_ptr(), uv.data_ptr(), 70, 90,
+                                     d["k"].data_ptr(), 33, 1, 1, 1, 1, 1, traced.data_ptr(),
+                                     None, stream, 0))
+    _native.check(lib.rlic_replay_f32(tex2.data_ptr(), codes.data_ptr(), 70, 90,
+                                      d["k"].data_ptr(), 33, out.data_ptr(), stream, 0))
+    assert_bitwise(out.cpu().numpy(), traced.cpu().numpy())
+    want2 = oracle.convolve(tex2.cpu().numpy(), u, v, k, uv_mode="polarization",
+                            boundaries="periodic")
+    assert_bitwise(out.cpu().numpy(), want2)
