@@ -136,6 +136,41 @@ RLIC_API int rlic_convolve_f64(const double *texture, const double *u, const dou
                       size_t workspace_bytes, void *stream, unsigned flags);
 
 /*
+ * rlic_convolve_f32 for callers that cannot allocate device memory: a plugin
+ * whose host application owns the whole device-memory budget and forbids
+ * its plugins from allocating, code that runs inside another library's
+ * allocator callback (where calling back into the allocator would
+ * deadlock), or a latency-critical loop that cannot afford the device-wide
+ * synchronisation cudaMalloc and cudaFree can cause.  No counterpart in the
+ * reference, whose native core allocates its own buffers on the host.
+ *
+ * Same arguments, results and flags as rlic_convolve_f32 with device
+ * pointers, minus the workspace: the call allocates nothing (no cudaMalloc,
+ * cudaMallocAsync or cudaFree) and uses a static device array of
+ * RLIC_NOALLOC_SCRATCH_BYTES (64 MiB) instead.  The caller still provides
+ * texture, u, v, kernel and out.  A call whose rlic_workspace_bytes(ny, nx,
+ * klen, iterations, 4, flags) exceeds that size fails with
+ * RLIC_ERR_WORKSPACE_TOO_SMALL before touching the GPU;
+ * RLIC_FLAG_NO_PATH_CACHE shrinks the need to about 12 bytes per pixel.
+ * RLIC_FLAG_HOST_MEMORY is rejected.
+ *
+ * The array belongs to the library's module, so every GPU that loads the
+ * library holds it until the process exits.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the one array: calls whose work overlaps on the GPU (different
+ * streams, or different host threads on one device) race and must be
+ * serialised by the caller.  Each call writes every part of the array it
+ * reads, so the previous call's contents never leak into a result.
+ */
+#define RLIC_NOALLOC_SCRATCH_BYTES (64u << 20)
+RLIC_API int rlic_convolve_f32_noalloc(const float *texture, const float *u, const float *v,
+                                       int64_t ny, int64_t nx, const float *kernel,
+                                       int64_t klen, int uv_mode, int bx_left, int bx_right,
+                                       int by_left, int by_right, int64_t iterations,
+                                       float *out, void *stream, unsigned flags);
+
+/*
  * Streamline cells, for index-for-index parity checks of the trace
  * (convole_single_pixel, src/lib.rs:305-362; advance, src/lib.rs:236-273).
  *

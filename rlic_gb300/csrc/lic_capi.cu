@@ -25,6 +25,7 @@
 #include "lic_launch.h"
 
 #include <atomic>
+#include <mutex>
 #include <string>
 
 namespace rlic {
@@ -363,6 +364,67 @@ int replay_impl(const T* tex_in, const void* codes, int64_t ny, int64_t nx, cons
     return RLIC_OK;
 }
 
+// ------------------------------------------------------- no-allocation path --
+//
+// Scratch of rlic_convolve_f32_noalloc, for callers that cannot allocate
+// device memory themselves (see the header).  It is a file-scope device
+// array, so the module holds it on every GPU that loads this library, for
+// the life of the process.  In host code the array's name only stands for
+// the symbol; its device address comes from cudaGetSymbolAddress, resolved
+// once per device (with that device current) and cached.
+constexpr size_t kStaticScratchBytes = size_t(RLIC_NOALLOC_SCRATCH_BYTES);
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {};
+
+int static_scratch(unsigned char** ptr) {
+    int dev = -1;
+    RLIC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "device ordinal out of range for static scratch");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (g_static_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        RLIC_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+        g_static_ptr[dev] = p;
+    }
+    *ptr = static_cast<unsigned char*>(g_static_ptr[dev]);
+    return RLIC_OK;
+}
+
+int convolve_noalloc_f32(const float* texture, const float* u, const float* v, int64_t ny,
+                         int64_t nx, const float* kernel, int64_t klen, int uv_mode, int bxl,
+                         int bxr, int byl, int byr, int64_t iterations, float* out,
+                         void* stream_, unsigned flags) {
+    g_last_error.clear();
+    const int bnd[4] = {bxl, bxr, byl, byr};
+    int rc = check_common(ny, nx, klen, uv_mode, bnd, flags);
+    if (rc) return rc;
+    if (flags & RLIC_FLAG_HOST_MEMORY)
+        return fail(RLIC_ERR_INVALID_ARGUMENT,
+                    "rlic_convolve_f32_noalloc takes device pointers only");
+    if (iterations < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "iterations must be >= 0");
+    if (!texture || !u || !v || !kernel || !out)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    const WorkspaceLayout wl = workspace_layout(ny, nx, klen, iterations, sizeof(float), flags);
+    if (wl.total > kStaticScratchBytes)
+        return fail(RLIC_ERR_WORKSPACE_TOO_SMALL,
+                    "this call needs " + std::to_string(wl.total) +
+                        " bytes of scratch; the static scratch holds " +
+                        std::to_string(kStaticScratchBytes) +
+                        " (use a smaller image, fewer taps, or RLIC_FLAG_NO_PATH_CACHE)");
+    unsigned char* ws = nullptr;
+    rc = static_scratch(&ws);
+    if (rc) return rc;
+    // Every region of the scratch is written before it is read (packed field,
+    // ping-pong buffer, path codes), so the previous call's contents need no
+    // clearing.
+    return run_device<float>(texture, u, v, ny, nx, kernel, klen, make_variant(flags, uv_mode),
+                             bnd, iterations, out, ws, flags, static_cast<cudaStream_t>(stream_));
+}
+
 }  // namespace
 
 // -------------------------------------------------------------------- C ABI --
@@ -455,6 +517,14 @@ int rlic_replay_f64(const double* tex_in, const void* codes, int64_t ny, int64_t
                     const double* kernel, int64_t klen, double* tex_out, void* stream,
                     unsigned flags) {
     return replay_impl<double>(tex_in, codes, ny, nx, kernel, klen, tex_out, stream, flags);
+}
+
+int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float* v,
+                              int64_t ny, int64_t nx, const float* kernel, int64_t klen,
+                              int uv_mode, int bx_left, int bx_right, int by_left, int by_right,
+                              int64_t iterations, float* out, void* stream, unsigned flags) {
+    return convolve_noalloc_f32(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left, bx_right,
+                                by_left, by_right, iterations, out, stream, flags);
 }
 
 int rlic_set_block_shape(int block_x, int block_y) {
