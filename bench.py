@@ -66,6 +66,10 @@ def parse_args() -> argparse.Namespace:
                    help="target CPU time of the oracle baseline sample")
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=["fourier", "readme", "precision"], default="fourier",
+                   help="fourier: the headline 8192^2 float32 case (default); readme: the "
+                        "reference's README case, 256^2 float64; precision: 8192^2 float64, "
+                        "K=129, 10 iterations, exact vs FP16/BF16 storage forms")
     return p.parse_args()
 
 
@@ -485,13 +489,150 @@ def run_gb300(args, dist: Dist) -> None:
     dist.close()
 
 
+# ------------------------------------------------------- other workloads --
+
+def _time_calls(fn, steps: int, warmup: int, stream) -> float:
+    """Mean ms per call of fn() (CUDA events on `stream`)."""
+    import torch
+
+    for _ in range(max(1, warmup)):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def run_readme(args) -> None:
+    """The reference's README case: 256^2 float64, K=65, periodic, velocity, n=1."""
+    import torch
+
+    import rlic_gb300
+    from oracle import oracle
+    from rlic_gb300 import _native
+    from rlic_gb300.workloads import readme_case
+
+    c = readme_case()
+    lib = _native.lib()
+    n, klen = 256, 65
+    dev = torch.device("cuda", 0)
+    t = {x: torch.from_numpy(np.ascontiguousarray(c[x])).to(dev) for x in ("texture", "u", "v", "kernel")}
+    out = torch.empty_like(t["texture"])
+    nbytes = lib.rlic_workspace_bytes(n, n, klen, 1, 8, 0)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def call():
+        _native.check(lib.rlic_convolve_f64(
+            t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), n, n,
+            t["kernel"].data_ptr(), klen, 0, 1, 1, 1, 1, 1, out.data_ptr(), ws.data_ptr(),
+            nbytes, sp, 0))
+
+    steps = max(args.steps, 50)
+    ms = _time_calls(call, steps, args.warmup, stream)
+    samples = n * n * klen
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], boundaries="periodic")
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
+    res = {}
+    for threads in (1, oracle.env_threads()):
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], boundaries="periodic",
+                            nthreads=threads)
+        res[threads] = samples * reps / (time.perf_counter() - t0) / 1e9
+    print(json.dumps({
+        "metric": METRIC, "unit": UNIT, "workload": "readme_256x256_f64_triangle65_periodic_velocity_n1",
+        "value": samples / (ms / 1e3) / 1e9, "ms_per_call": ms, "dtype": "f64", "steps": steps,
+        "e2e": {"value": samples / (e2e_ms / 1e3) / 1e9, "ms_per_call": e2e_ms},
+        "cpu_oracle_gsamples": {f"{k}_threads": v for k, v in res.items()},
+    }), flush=True)
+
+
+def run_precision(args) -> None:
+    """8192^2 float64 (README recipe, seed 2), K=129 triangle, periodic, n=10:
+    the exact plain and path-cache forms against the FP16 / BF16 storage forms."""
+    import torch
+
+    from rlic_gb300 import _native
+    from rlic_gb300.workloads import readme_case
+
+    n, klen, iters = args.size, 129, 10
+    c = readme_case(n=n, klen=klen, dtype=np.float64, seed=2)
+    dev = torch.device("cuda", 0)
+    t = {x: torch.from_numpy(np.ascontiguousarray(c[x])).to(dev) for x in ("texture", "u", "v", "kernel")}
+    lib = _native.lib()
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    samples = n * n * klen * iters
+    outs, times = {}, {}
+    for name, flags in (("f64_plain", _native.RLIC_FLAG_NO_PATH_CACHE), ("f64_path_cache", 0)):
+        out = torch.empty_like(t["texture"])
+        nbytes = lib.rlic_workspace_bytes(n, n, klen, iters, 8, flags)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+        def call(out=out, ws=ws, nbytes=nbytes, flags=flags):
+            _native.check(lib.rlic_convolve_f64(
+                t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), n, n,
+                t["kernel"].data_ptr(), klen, 0, 1, 1, 1, 1, iters, out.data_ptr(),
+                ws.data_ptr(), nbytes, sp, flags))
+
+        times[name] = _time_calls(call, 2 if "plain" in name else 3, 1, stream)
+        outs[name] = out
+        del ws
+    for name, st in (("fp16", _native.RLIC_STORAGE_FP16), ("bf16", _native.RLIC_STORAGE_BF16)):
+        out = torch.empty_like(t["texture"])
+        nbytes = lib.rlic_lowp_workspace_bytes(n, n, klen, 8)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+        def call(out=out, ws=ws, nbytes=nbytes, st=st):
+            _native.check(lib.rlic_convolve_lowp_f64(
+                t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), n, n,
+                t["kernel"].data_ptr(), klen, 0, 1, 1, 1, 1, iters, st, out.data_ptr(),
+                ws.data_ptr(), nbytes, sp, 0))
+
+        times[name] = _time_calls(call, 3, 1, stream)
+        outs[name] = out
+        del ws
+    exact = outs["f64_plain"]
+    assert torch.equal(exact, outs["f64_path_cache"]), "path-cache form differs from plain"
+    scale = float(torch.sum(torch.abs(t["kernel"]))) ** iters
+    errs = {}
+    for name in ("fp16", "bf16"):
+        d = (outs[name] - exact) / scale
+        errs[name] = {"max_abs": float(d.abs().max()), "rms": float(torch.sqrt((d * d).mean()))}
+    forms = {k: {"ms_per_step": v, "value": samples / (v / 1e3) / 1e9} for k, v in times.items()}
+    for k in ("fp16", "bf16"):
+        forms[k]["error_vs_f64_normalised"] = errs[k]
+        forms[k]["speedup_vs_f64_plain"] = times["f64_plain"] / times[k]
+        forms[k]["speedup_vs_f64_path_cache"] = times["f64_path_cache"] / times[k]
+    print(json.dumps({
+        "metric": METRIC, "unit": UNIT,
+        "workload": f"readme_recipe_{n}x{n}_f64_triangle{klen}_periodic_velocity_n{iters}",
+        "value": forms["fp16"]["value"], "dtype": "f64 in, fp16 storage",
+        "forms": forms, "error_normalisation": "outputs divided by sum(|kernel|)^iterations",
+    }), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
         return
-    run_gb300(args, dist)
+    if args.workload == "readme":
+        run_readme(args)
+    elif args.workload == "precision":
+        run_precision(args)
+    else:
+        run_gb300(args, dist)
 
 
 if __name__ == "__main__":

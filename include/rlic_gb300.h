@@ -136,6 +136,40 @@ RLIC_API int rlic_convolve_f64(const double *texture, const double *u, const dou
                       size_t workspace_bytes, void *stream, unsigned flags);
 
 /*
+ * Reduced-precision form of rlic_convolve_* (device pointers, asynchronous).
+ *
+ * Streamline cells come from a trace in the input dtype (the cell choices are
+ * discontinuous in the arithmetic and need its precision); the texture and
+ * every buffer between passes are then stored as FP16 (RLIC_STORAGE_FP16) or
+ * BF16 (RLIC_STORAGE_BF16), each pass accumulates in FP32 with compensated
+ * (Kahan) summation and stores its output divided by sum(|kernel|), and the
+ * last buffer is scaled back in the input dtype into `out`.  Results are
+ * approximations of rlic_convolve_*: the error is that of 16-bit storage
+ * (relative 2^-11 for FP16, 2^-8 for BF16 per pass, before averaging).
+ * No counterpart in the reference.
+ *
+ * workspace: rlic_lowp_workspace_bytes(ny, nx, klen, 4 or 8) bytes, 256-byte
+ * aligned, or NULL to allocate stream-ordered.  `flags` takes the variant
+ * bits only.
+ */
+#define RLIC_STORAGE_FP16 0
+#define RLIC_STORAGE_BF16 1
+RLIC_API size_t rlic_lowp_workspace_bytes(int64_t ny, int64_t nx, int64_t klen,
+                                          int elem_bytes);
+RLIC_API int rlic_convolve_lowp_f32(const float *texture, const float *u, const float *v,
+                                    int64_t ny, int64_t nx, const float *kernel, int64_t klen,
+                                    int uv_mode, int bx_left, int bx_right, int by_left,
+                                    int by_right, int64_t iterations, int storage, float *out,
+                                    void *workspace, size_t workspace_bytes, void *stream,
+                                    unsigned flags);
+RLIC_API int rlic_convolve_lowp_f64(const double *texture, const double *u, const double *v,
+                                    int64_t ny, int64_t nx, const double *kernel,
+                                    int64_t klen, int uv_mode, int bx_left, int bx_right,
+                                    int by_left, int by_right, int64_t iterations, int storage,
+                                    double *out, void *workspace, size_t workspace_bytes,
+                                    void *stream, unsigned flags);
+
+/*
  * rlic_convolve_f32 for callers that cannot allocate device memory: a plugin
  * whose host application owns the whole device-memory budget and forbids
  * its plugins from allocating, code that runs inside another library's

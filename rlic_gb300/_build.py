@@ -42,7 +42,7 @@ NVCC_FLAGS = [
     "-warn-spills",
 ]
 
-SOURCES = ["lic_capi.cu", "lic_kernels_f32.cu", "lic_kernels_f64.cu"]
+SOURCES = ["lic_capi.cu", "lic_kernels_f32.cu", "lic_kernels_f64.cu", "lic_lowp.cu"]
 
 
 def nvcc_path() -> str:

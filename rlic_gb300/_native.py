@@ -28,6 +28,9 @@ RLIC_FLAG_NO_FMA = 0x2
 RLIC_FLAG_NO_BRANCHLESS = 0x4
 RLIC_FLAG_NO_PATH_CACHE = 0x8
 
+RLIC_STORAGE_FP16 = 0
+RLIC_STORAGE_BF16 = 1
+
 # size of the static scratch of rlic_convolve_f32_noalloc (RLIC_NOALLOC_SCRATCH_BYTES)
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -62,6 +65,11 @@ SIGNATURES: dict[str, tuple[list, object]] = {
                         _U], _INT),
     "rlic_replay_f32": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
     "rlic_replay_f64": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
+    "rlic_lowp_workspace_bytes": ([_I64, _I64, _I64, _INT], _SZ),
+    "rlic_convolve_lowp_f32": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT,
+                                _I64, _INT, _P, _P, _SZ, _P, _U], _INT),
+    "rlic_convolve_lowp_f64": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT,
+                                _I64, _INT, _P, _P, _SZ, _P, _U], _INT),
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),

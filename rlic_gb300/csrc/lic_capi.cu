@@ -47,8 +47,8 @@ using rlic::Shape;
 using rlic::Variant;
 
 thread_local std::string g_last_error;
-std::atomic<int> g_block_x{32};
-std::atomic<int> g_block_y{8};
+std::atomic<int> g_block_x{64};
+std::atomic<int> g_block_y{4};
 
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
@@ -162,8 +162,9 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     for (int64_t it = 0; it < iterations; ++it) {
         T* dst = ((iterations - 1 - it) % 2 == 0) ? out : tmp;
         if (it == 0 || !cache) {
-            RLIC_CUDA_TRY(rlic::launch_pass(var, cache, src, uv, kernel, int(klen), sh, lc, dst,
-                                            codes, stream));
+            RLIC_CUDA_TRY(rlic::launch_pass(var, cache ? rlic::kPassSampleRecord : rlic::kPassSample,
+                                            src, uv, kernel, int(klen), sh, lc, dst, codes,
+                                            stream));
         } else {
             RLIC_CUDA_TRY(rlic::launch_gather(var.fma, src, codes, kernel, int(klen), sh, lc,
                                               dst, stream));
@@ -337,8 +338,11 @@ int sweep_impl(const T* tex_in, const void* uv, int64_t ny, int64_t nx, const T*
     if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
     const Variant var = make_variant(flags, uv_mode);
-    RLIC_CUDA_TRY(rlic::launch_pass(var, codes != nullptr && klen > 1, tex_in, uv, kernel,
-                                    int(klen), make_shape(ny, nx, bnd), launch_config(), tex_out,
+    RLIC_CUDA_TRY(rlic::launch_pass(var,
+                                    (codes != nullptr && klen > 1) ? rlic::kPassSampleRecord
+                                                                   : rlic::kPassSample,
+                                    tex_in, uv, kernel, int(klen), make_shape(ny, nx, bnd),
+                                    launch_config(), tex_out,
                                     static_cast<uint32_t*>(codes),
                                     static_cast<cudaStream_t>(stream_)));
     return RLIC_OK;
@@ -362,6 +366,100 @@ int replay_impl(const T* tex_in, const void* codes, int64_t ny, int64_t nx, cons
                                       make_shape(ny, nx, bnd), launch_config(), tex_out,
                                       static_cast<cudaStream_t>(stream_)));
     return RLIC_OK;
+}
+
+// -------------------------------------------------- reduced-precision form --
+
+struct LowpLayout {
+    size_t uv, codes, buf_a, buf_b, w32, scal, total;
+};
+
+LowpLayout lowp_layout(int64_t ny, int64_t nx, int64_t klen, size_t s) {
+    const size_t n = size_t(ny) * size_t(nx);
+    LowpLayout w{};
+    size_t off = 0;
+    w.uv = off;
+    off += align_up(2 * n * s);
+    w.codes = off;
+    off += align_up(code_bytes(ny, nx, klen));
+    w.buf_a = off;
+    off += align_up(2 * n);
+    w.buf_b = off;
+    off += align_up(2 * n);
+    w.w32 = off;
+    off += align_up(size_t(klen) * 4);
+    w.scal = off;  // float 1/sum(|kernel|) at +0, double undo factor at +8
+    off += align_up(16);
+    w.total = off;
+    return w;
+}
+
+template <typename T>
+int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
+                       const T* kernel, int64_t klen, int uv_mode, int bxl, int bxr, int byl,
+                       int byr, int64_t iterations, int storage, T* out, void* workspace,
+                       size_t workspace_bytes_, void* stream_, unsigned flags) {
+    g_last_error.clear();
+    const int bnd[4] = {bxl, bxr, byl, byr};
+    int rc = check_common(ny, nx, klen, uv_mode, bnd, flags);
+    if (rc) return rc;
+    if (flags & (RLIC_FLAG_HOST_MEMORY | RLIC_FLAG_NO_PATH_CACHE))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes the variant flags only");
+    if (storage != RLIC_STORAGE_FP16 && storage != RLIC_STORAGE_BF16)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "storage must be RLIC_STORAGE_FP16 or _BF16");
+    if (iterations < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "iterations must be >= 0");
+    if (!texture || !u || !v || !kernel || !out)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    const int64_t n = ny * nx;
+    if (iterations == 0) {
+        RLIC_CUDA_TRY(cudaMemsetAsync(out, 0, size_t(n) * sizeof(T), stream));
+        return RLIC_OK;
+    }
+    const LowpLayout wl = lowp_layout(ny, nx, klen, sizeof(T));
+    unsigned char* ws = static_cast<unsigned char*>(workspace);
+    bool owned = false;
+    if (ws == nullptr) {
+        RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&ws), wl.total, stream));
+        owned = true;
+    } else {
+        if (workspace_bytes_ < wl.total)
+            return fail(RLIC_ERR_WORKSPACE_TOO_SMALL,
+                        "workspace smaller than rlic_lowp_workspace_bytes()");
+        if (reinterpret_cast<uintptr_t>(ws) % kAlign != 0)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    }
+    auto body = [&]() -> int {
+        const Shape sh = make_shape(ny, nx, bnd);
+        const LaunchConfig lc = launch_config();
+        void* uv = ws + wl.uv;
+        uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
+        float* w32 = reinterpret_cast<float*>(ws + wl.w32);
+        float* inv_scale = reinterpret_cast<float*>(ws + wl.scal);
+        double* undo = reinterpret_cast<double*>(ws + wl.scal + 8);
+        void* bufs[2] = {ws + wl.buf_a, ws + wl.buf_b};
+        RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream));
+        RLIC_CUDA_TRY(rlic::launch_pass(make_variant(flags, uv_mode), rlic::kPassRecordOnly,
+                                        static_cast<const T*>(nullptr), uv, kernel, int(klen), sh,
+                                        lc, static_cast<T*>(nullptr), codes, stream));
+        RLIC_CUDA_TRY(rlic::launch_lowp_prepare(kernel, int(klen), iterations, w32, inv_scale,
+                                                undo, stream));
+        RLIC_CUDA_TRY(rlic::launch_to_storage(texture, bufs[0], storage, n, stream));
+        for (int64_t it = 0; it < iterations; ++it) {
+            RLIC_CUDA_TRY(rlic::launch_gather_lowp(storage, bufs[it % 2], codes, w32, int(klen),
+                                                   inv_scale, sh, lc, bufs[(it + 1) % 2],
+                                                   stream));
+        }
+        RLIC_CUDA_TRY(rlic::launch_from_storage(bufs[iterations % 2], storage, undo, out, n,
+                                                stream));
+        return RLIC_OK;
+    };
+    rc = body();
+    if (owned) {
+        cudaError_t e = cudaFreeAsync(ws, stream);
+        if (rc == RLIC_OK && e != cudaSuccess) return cuda_fail(e, "cudaFreeAsync");
+    }
+    return rc;
 }
 
 // ------------------------------------------------------- no-allocation path --
@@ -517,6 +615,32 @@ int rlic_replay_f64(const double* tex_in, const void* codes, int64_t ny, int64_t
                     const double* kernel, int64_t klen, double* tex_out, void* stream,
                     unsigned flags) {
     return replay_impl<double>(tex_in, codes, ny, nx, kernel, klen, tex_out, stream, flags);
+}
+
+size_t rlic_lowp_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int elem_bytes) {
+    if (elem_bytes != 4 && elem_bytes != 8) return 0;
+    if (ny <= 0 || nx <= 0 || klen <= 0) return 0;
+    return lowp_layout(ny, nx, klen, size_t(elem_bytes)).total;
+}
+
+int rlic_convolve_lowp_f32(const float* texture, const float* u, const float* v, int64_t ny,
+                           int64_t nx, const float* kernel, int64_t klen, int uv_mode,
+                           int bx_left, int bx_right, int by_left, int by_right,
+                           int64_t iterations, int storage, float* out, void* workspace,
+                           size_t workspace_bytes, void* stream, unsigned flags) {
+    return convolve_lowp_impl<float>(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left,
+                                     bx_right, by_left, by_right, iterations, storage, out,
+                                     workspace, workspace_bytes, stream, flags);
+}
+
+int rlic_convolve_lowp_f64(const double* texture, const double* u, const double* v, int64_t ny,
+                           int64_t nx, const double* kernel, int64_t klen, int uv_mode,
+                           int bx_left, int bx_right, int by_left, int by_right,
+                           int64_t iterations, int storage, double* out, void* workspace,
+                           size_t workspace_bytes, void* stream, unsigned flags) {
+    return convolve_lowp_impl<double>(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left,
+                                      bx_right, by_left, by_right, iterations, storage, out,
+                                      workspace, workspace_bytes, stream, flags);
 }
 
 int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float* v,

@@ -26,6 +26,9 @@
 // takes the interior path without boundary logic.
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "lic_device.cuh"
 #include "lic_launch.h"
 
@@ -92,26 +95,34 @@ struct CodeLayout {
     int words_f;  // ceil(nf / 8)
 };
 
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, bool RECORD, typename I>
+// What a traced pass does with each step: sample the texture (kSample),
+// sample and record the step codes (kSampleRecord), or only record them
+// (kRecordOnly, no texture read and no output).
+enum PassMode : int { kSample = 0, kSampleRecord = 1, kRecordOnly = 2 };
+
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, int MODE, typename I>
 __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
                                             const typename Vec2<T>::type* __restrict__ uv,
                                             const T* __restrict__ tex, const T* wf, const T* wb,
                                             T wmid, int nf, int kmid, uint32_t* __restrict__ codes,
                                             const CodeLayout& cl) {
+    constexpr bool SAMPLE = MODE != kRecordOnly;
+    constexpr bool RECORD = MODE != kSample;
     const I p = i * g.nx + j;
-    T acc = accumulate<T, FMA>(wmid, __ldg(tex + p), T(0));
+    T acc = T(0);
+    if constexpr (SAMPLE) acc = accumulate<T, FMA>(wmid, __ldg(tex + p), T(0));
     uint32_t* words_f = RECORD ? codes + p : nullptr;
     uint32_t* words_b = RECORD ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : nullptr;
-    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, true, RECORD>(acc, i, j, g, uv, tex, wf,
-                                                                   nf, words_f, cl.npix);
-    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, true, RECORD>(acc, i, j, g, uv, tex, wb,
-                                                                  kmid, words_b, cl.npix);
+    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD>(acc, i, j, g, uv, tex, wf,
+                                                                     nf, words_f, cl.npix);
+    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD>(acc, i, j, g, uv, tex, wb,
+                                                                    kmid, words_b, cl.npix);
     return acc;
 }
 
 // One convolution pass, one pixel tile per CTA (the hardware balances CTAs of
 // uneven cost, e.g. streamlines that stop early).
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool RECORD, typename I>
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
 __global__ void __launch_bounds__(256, PassMinBlocks<T>::value)
 lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __restrict__ uv,
                 const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
@@ -121,21 +132,27 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
     const int kmid = klen / 2;
     const int nf = klen - kmid - 1;
     const int nf_pad = (nf + 7) & ~7;
-    load_step_weights(wsm, kernel, klen, nf_pad);
-    __syncthreads();
-    const T wmid = __ldg(kernel + kmid);
+    if constexpr (MODE != kRecordOnly) {
+        load_step_weights(wsm, kernel, klen, nf_pad);
+        __syncthreads();
+    }
+    const T wmid = (MODE != kRecordOnly) ? __ldg(kernel + kmid) : T(0);
     const I tile = I(blockIdx.x);
     const I ti = tile / tg.tiles_x;
     const I tj = tile - ti * tg.tiles_x;
     const I i = ti * tg.by + I(threadIdx.y);
     const I j = tj * tg.bx + I(threadIdx.x);
+    T acc;
     if (tile_is_interior(ti, tj, tg, g)) {
-        tex_out[i * g.nx + j] = convolve_pixel<T, FMA, BRANCHLESS, POL, false, RECORD>(
+        acc = convolve_pixel<T, FMA, BRANCHLESS, POL, false, MODE>(
             i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
     } else if (i < g.ny && j < g.nx) {
-        tex_out[i * g.nx + j] = convolve_pixel<T, FMA, BRANCHLESS, POL, true, RECORD>(
+        acc = convolve_pixel<T, FMA, BRANCHLESS, POL, true, MODE>(
             i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+    } else {
+        return;
     }
+    if constexpr (MODE != kRecordOnly) tex_out[i * g.nx + j] = acc;
 }
 
 // True when one of the 8 codes of a word is the stop code (all four bits set).
@@ -143,37 +160,62 @@ __device__ __forceinline__ bool word_has_stop(uint32_t wd) {
     return (wd & (wd >> 1) & (wd >> 2) & (wd >> 3) & 0x11111111u) != 0u;
 }
 
-// Replays `count` recorded steps of one half from pixel p.  Words without a
-// stop code (all of them unless the field holds NaNs) run branch-free: the 8
-// deltas, the 8 cells and the 8 texture loads are independent of the
-// accumulation, so they are all in flight before the 8 ordered FMAs.
+// Replays `count` recorded steps of one half from pixel p.  A word holds 8
+// steps.  Words without a stop code (all of them unless the field holds
+// NaNs) are gathered branch-free, and one word ahead: the 8 texture loads of
+// word q+1 are in flight while the 8 ordered FMAs of word q run, so the
+// accumulation order (that of the traced pass) is kept while the load
+// latency is hidden.
+template <typename T, typename I>
+__device__ __forceinline__ void gather8(I& cell, uint32_t wd, const I* table,
+                                        const T* __restrict__ tex, T x[8]) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        cell += table[(wd >> (4 * b)) & 15u];
+        x[b] = __ldg(tex + cell);
+    }
+}
+
 template <typename T, bool FMA, typename I>
 __device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restrict__ words,
                                             int64_t npix, int count, const T* w, const I* table,
                                             const T* __restrict__ tex) {
     I cell = p;
     const int full = count >> 3;
-    for (int q = 0; q <= full; ++q) {
+    int q = 0;
+    // pipelined run of full words without stop codes
+    if (full > 0) {
+        uint32_t wd = __ldg(words);
+        if (!word_has_stop(wd)) {
+            T x[8];
+            gather8<T, I>(cell, wd, table, tex, x);
+            for (q = 1; q < full; ++q) {
+                wd = __ldg(words + size_t(q) * size_t(npix));
+                if (word_has_stop(wd)) break;
+                T y[8];
+                gather8<T, I>(cell, wd, table, tex, y);
+                const T* wq = w + 8 * (q - 1);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) x[b] = y[b];
+            }
+            const T* wq = w + 8 * (q - 1);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
+        }
+    }
+    // remaining steps one by one: a word with a stop code, or the last partial word
+    for (; q <= full; ++q) {
         const int n = (q < full) ? 8 : (count & 7);
         if (n == 0) break;
         const uint32_t wd = __ldg(words + size_t(q) * size_t(npix));
         const T* wq = w + 8 * q;
-        if (n == 8 && !word_has_stop(wd)) {
-            T x[8];
-#pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                cell += table[(wd >> (4 * b)) & 15u];
-                x[b] = __ldg(tex + cell);
-            }
-#pragma unroll
-            for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
-        } else {
-            for (int b = 0; b < n; ++b) {
-                const uint32_t code = (wd >> (4 * b)) & 15u;
-                if (code == kStop) return;
-                cell += table[code];
-                acc = accumulate<T, FMA>(wq[b], __ldg(tex + cell), acc);
-            }
+        for (int b = 0; b < n; ++b) {
+            const uint32_t code = (wd >> (4 * b)) & 15u;
+            if (code == kStop) return;
+            cell += table[code];
+            acc = accumulate<T, FMA>(wq[b], __ldg(tex + cell), acc);
         }
     }
 }
@@ -229,6 +271,67 @@ __global__ void trace_cells_kernel(const typename Vec2<T>::type* __restrict__ uv
                                               [dst](int s, int64_t c) { dst[s] = c; });
     walk_half<T, FMA, BRANCHLESS, POL, true>(i, j, g, uv, kmid,
                                              [dst, nf](int s, int64_t c) { dst[nf + s] = c; });
+}
+
+// ------------------------------------------------ reduced-precision helpers --
+
+// Float copy of the kernel, 1/sum(|kernel|) as used by the reduced-precision
+// replays, and the factor that undoes `iterations` of those normalisations
+// (computed from the float factor actually applied).  One CTA of 256 threads.
+template <typename T>
+__global__ void lowp_prepare_kernel(const T* __restrict__ kernel, int klen, int64_t iterations,
+                                    float* __restrict__ w32, float* __restrict__ inv_scale,
+                                    double* __restrict__ undo) {
+    __shared__ double part[256];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < klen; k += blockDim.x) {
+        w32[k] = float(kernel[k]);
+        s += fabs(double(kernel[k]));
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (int(threadIdx.x) < h) part[threadIdx.x] += part[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double total = part[0];
+        if (!(total > 0.0) || !isfinite(total)) total = 1.0;
+        const float inv = float(1.0 / total);
+        inv_scale[0] = inv;
+        undo[0] = pow(1.0 / double(inv), double(iterations));
+    }
+}
+
+__device__ __forceinline__ __half to_half(float x) { return __float2half_rn(x); }
+__device__ __forceinline__ __half to_half(double x) { return __double2half(x); }
+__device__ __forceinline__ __nv_bfloat16 to_bf16(float x) { return __float2bfloat16_rn(x); }
+__device__ __forceinline__ __nv_bfloat16 to_bf16(double x) { return __double2bfloat16(x); }
+
+template <typename T>
+__global__ void to_storage_kernel(const T* __restrict__ src, void* __restrict__ dst, int storage,
+                                  int64_t n) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        if (storage == kStorageFP16)
+            static_cast<__half*>(dst)[k] = to_half(src[k]);
+        else
+            static_cast<__nv_bfloat16*>(dst)[k] = to_bf16(src[k]);
+    }
+}
+
+template <typename T>
+__global__ void from_storage_kernel(const void* __restrict__ src, int storage,
+                                    const double* __restrict__ undo, T* __restrict__ dst,
+                                    int64_t n) {
+    const double f = *undo;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const float x = (storage == kStorageFP16)
+                            ? __half2float(static_cast<const __half*>(src)[k])
+                            : __bfloat162float(static_cast<const __nv_bfloat16*>(src)[k]);
+        dst[k] = T(double(x) * f);
+    }
 }
 
 // ---------------------------------------------------------------- launchers --
@@ -305,16 +408,16 @@ cudaError_t launch_pack_t(const T* u, const T* v, void* uv, int64_t n, cudaStrea
     return cudaGetLastError();
 }
 
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool RECORD, typename I>
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
 cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int klen,
                           const Shape& sh, const LaunchConfig& lc, T* tex_out, uint32_t* codes,
                           cudaStream_t stream) {
     const auto g = make_geometry<I>(sh);
     const auto tg = make_tiles<I>(sh, lc, klen);
     const auto cl = make_code_layout(sh, klen);
-    const size_t smem = weights_smem_bytes(klen, sizeof(T));
+    const size_t smem = (MODE == kRecordOnly) ? 0 : weights_smem_bytes(klen, sizeof(T));
     if (int64_t(tg.ntiles) > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    auto kfn = lic_pass_kernel<T, FMA, BRANCHLESS, POL, RECORD, I>;
+    auto kfn = lic_pass_kernel<T, FMA, BRANCHLESS, POL, MODE, I>;
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -327,35 +430,44 @@ cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int 
     return cudaGetLastError();
 }
 
-template <typename T, typename I>
-cudaError_t launch_pass_i(const Variant& var, bool record, const T* tex_in, const void* uv,
-                          const T* kernel, int klen, const Shape& sh, const LaunchConfig& lc,
-                          T* tex_out, uint32_t* codes, cudaStream_t stream) {
-    const int code = (var.fma ? 8 : 0) | (var.branchless ? 4 : 0) | (var.pol ? 2 : 0) |
-                     (record ? 1 : 0);
-#define RLIC_PASS_CASE(C, F, B, P, R)                                                      \
-    case C:                                                                                \
-        return launch_pass_t<T, F, B, P, R, I>(tex_in, uv, kernel, klen, sh, lc, tex_out,  \
-                                               codes, stream);
+template <typename T, int MODE, typename I>
+cudaError_t launch_pass_m(const Variant& var, const T* tex_in, const void* uv, const T* kernel,
+                          int klen, const Shape& sh, const LaunchConfig& lc, T* tex_out,
+                          uint32_t* codes, cudaStream_t stream) {
+    const int code = (var.fma ? 4 : 0) | (var.branchless ? 2 : 0) | (var.pol ? 1 : 0);
+#define RLIC_PASS_CASE(C, F, B, P)                                                          \
+    case C:                                                                                 \
+        return launch_pass_t<T, F, B, P, MODE, I>(tex_in, uv, kernel, klen, sh, lc, tex_out, \
+                                                  codes, stream);
     switch (code) {
-        RLIC_PASS_CASE(0, false, false, false, false)
-        RLIC_PASS_CASE(1, false, false, false, true)
-        RLIC_PASS_CASE(2, false, false, true, false)
-        RLIC_PASS_CASE(3, false, false, true, true)
-        RLIC_PASS_CASE(4, false, true, false, false)
-        RLIC_PASS_CASE(5, false, true, false, true)
-        RLIC_PASS_CASE(6, false, true, true, false)
-        RLIC_PASS_CASE(7, false, true, true, true)
-        RLIC_PASS_CASE(8, true, false, false, false)
-        RLIC_PASS_CASE(9, true, false, false, true)
-        RLIC_PASS_CASE(10, true, false, true, false)
-        RLIC_PASS_CASE(11, true, false, true, true)
-        RLIC_PASS_CASE(12, true, true, false, false)
-        RLIC_PASS_CASE(13, true, true, false, true)
-        RLIC_PASS_CASE(14, true, true, true, false)
-        RLIC_PASS_CASE(15, true, true, true, true)
+        RLIC_PASS_CASE(0, false, false, false)
+        RLIC_PASS_CASE(1, false, false, true)
+        RLIC_PASS_CASE(2, false, true, false)
+        RLIC_PASS_CASE(3, false, true, true)
+        RLIC_PASS_CASE(4, true, false, false)
+        RLIC_PASS_CASE(5, true, false, true)
+        RLIC_PASS_CASE(6, true, true, false)
+        RLIC_PASS_CASE(7, true, true, true)
     }
 #undef RLIC_PASS_CASE
+    return cudaErrorInvalidValue;
+}
+
+template <typename T, typename I>
+cudaError_t launch_pass_i(const Variant& var, int mode, const T* tex_in, const void* uv,
+                          const T* kernel, int klen, const Shape& sh, const LaunchConfig& lc,
+                          T* tex_out, uint32_t* codes, cudaStream_t stream) {
+    switch (mode) {
+        case kSample:
+            return launch_pass_m<T, kSample, I>(var, tex_in, uv, kernel, klen, sh, lc, tex_out,
+                                                codes, stream);
+        case kSampleRecord:
+            return launch_pass_m<T, kSampleRecord, I>(var, tex_in, uv, kernel, klen, sh, lc,
+                                                      tex_out, codes, stream);
+        case kRecordOnly:
+            return launch_pass_m<T, kRecordOnly, I>(var, tex_in, uv, kernel, klen, sh, lc,
+                                                    tex_out, codes, stream);
+    }
     return cudaErrorInvalidValue;
 }
 
@@ -364,8 +476,8 @@ cudaError_t launch_gather_t(const T* tex_in, const uint32_t* codes, const T* ker
                             const Shape& sh, const LaunchConfig& lc, T* tex_out,
                             cudaStream_t stream) {
     const auto g = make_geometry<I>(sh);
-    const auto tg = make_tiles<I>(sh, lc, klen);
     const auto cl = make_code_layout(sh, klen);
+    const auto tg = make_tiles<I>(sh, lc, klen);
     const size_t smem = weights_smem_bytes(klen, sizeof(T)) + 16 * sizeof(I);
     auto kfn = lic_gather_kernel<T, FMA, I>;
     unsigned grid = 0;
@@ -405,19 +517,49 @@ cudaError_t launch_trace_cells_t(const Variant& var, const void* uv, const Shape
     return cudaGetLastError();
 }
 
+inline unsigned stream_blocks(int64_t n) {
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    return unsigned(blocks < 1 ? 1 : blocks);
+}
+
+template <typename T>
+cudaError_t launch_lowp_prepare_t(const T* kernel, int klen, int64_t iterations, float* w32,
+                                  float* inv_scale, double* undo, cudaStream_t stream) {
+    lowp_prepare_kernel<T><<<1, 256, 0, stream>>>(kernel, klen, iterations, w32, inv_scale, undo);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_to_storage_t(const T* src, void* dst, int storage, int64_t n,
+                                cudaStream_t stream) {
+    to_storage_kernel<T><<<stream_blocks(n), 256, 0, stream>>>(src, dst, storage, n);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_from_storage_t(const void* src, int storage, const double* undo, T* dst,
+                                  int64_t n, cudaStream_t stream) {
+    from_storage_kernel<T><<<stream_blocks(n), 256, 0, stream>>>(src, storage, undo, dst, n);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // Definitions of the per-type overloads declared in lic_launch.h.
 #define RLIC_DEFINE_LAUNCHERS(T)                                                             \
     cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) { \
         return launch_pack_t<T>(u, v, uv, n, stream);                                        \
     }                                                                                        \
-    cudaError_t launch_pass(const Variant& var, bool record, const T* tex_in, const void* uv, \
+    cudaError_t launch_pass(const Variant& var, int mode, const T* tex_in, const void* uv,    \
                             const T* kernel, int klen, const Shape& sh,                      \
                             const LaunchConfig& lc, T* tex_out, uint32_t* codes,             \
                             cudaStream_t stream) {                                           \
         if (sh.small_index())                                                                \
-            return launch_pass_i<T, int32_t>(var, record, tex_in, uv, kernel, klen, sh, lc,  \
+            return launch_pass_i<T, int32_t>(var, mode, tex_in, uv, kernel, klen, sh, lc,    \
                                              tex_out, codes, stream);                        \
-        return launch_pass_i<T, int64_t>(var, record, tex_in, uv, kernel, klen, sh, lc,      \
+        return launch_pass_i<T, int64_t>(var, mode, tex_in, uv, kernel, klen, sh, lc,        \
                                          tex_out, codes, stream);                            \
     }                                                                                        \
     cudaError_t launch_gather(bool fma, const T* tex_in, const uint32_t* codes,              \
@@ -437,6 +579,20 @@ cudaError_t launch_trace_cells_t(const Variant& var, const void* uv, const Shape
                                    const Shape& sh, int klen, int64_t npix,                  \
                                    const int64_t* pix, int64_t* cells, cudaStream_t stream) { \
         return launch_trace_cells_t<T>(var, uv, sh, klen, npix, pix, cells, stream);         \
+    }                                                                                        \
+    cudaError_t launch_lowp_prepare(const T* kernel, int klen, int64_t iterations,           \
+                                    float* w32, float* inv_scale, double* undo,              \
+                                    cudaStream_t stream) {                                   \
+        return launch_lowp_prepare_t<T>(kernel, klen, iterations, w32, inv_scale, undo,      \
+                                        stream);                                             \
+    }                                                                                        \
+    cudaError_t launch_to_storage(const T* src, void* dst, int storage, int64_t n,           \
+                                  cudaStream_t stream) {                                     \
+        return launch_to_storage_t<T>(src, dst, storage, n, stream);                         \
+    }                                                                                        \
+    cudaError_t launch_from_storage(const void* src, int storage, const double* undo, T* dst, \
+                                    int64_t n, cudaStream_t stream) {                        \
+        return launch_from_storage_t<T>(src, storage, undo, dst, n, stream);                 \
     }
 
 }  // namespace rlic

@@ -31,6 +31,16 @@ struct LaunchConfig {
     int block_x, block_y;
 };
 
+// What a traced pass does per step: sample the texture, sample and record the
+// step codes, or record only (see lic_kernels.cuh).
+constexpr int kPassSample = 0;
+constexpr int kPassSampleRecord = 1;
+constexpr int kPassRecordOnly = 2;
+
+// Storage types of the reduced-precision form.
+constexpr int kStorageFP16 = 0;
+constexpr int kStorageBF16 = 1;
+
 // Counts one kernel launch (rlic_kernel_launch_count).
 void count_launch();
 
@@ -44,7 +54,7 @@ inline int64_t code_words_per_pixel(int64_t klen) {
 
 #define RLIC_DECLARE_LAUNCHERS(T)                                                          \
     cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream); \
-    cudaError_t launch_pass(const Variant& var, bool record, const T* tex_in, const void* uv, \
+    cudaError_t launch_pass(const Variant& var, int mode, const T* tex_in, const void* uv,    \
                             const T* kernel, int klen, const Shape& sh,                    \
                             const LaunchConfig& lc, T* tex_out, uint32_t* codes,           \
                             cudaStream_t stream);                                          \
@@ -53,10 +63,24 @@ inline int64_t code_words_per_pixel(int64_t klen) {
                               const LaunchConfig& lc, T* tex_out, cudaStream_t stream);    \
     cudaError_t launch_trace_cells(const Variant& var, const T* type_tag, const void* uv,  \
                                    const Shape& sh, int klen, int64_t npix,                \
-                                   const int64_t* pix, int64_t* cells, cudaStream_t stream);
+                                   const int64_t* pix, int64_t* cells, cudaStream_t stream); \
+    cudaError_t launch_lowp_prepare(const T* kernel, int klen, int64_t iterations,         \
+                                    float* w32, float* inv_scale, double* undo,            \
+                                    cudaStream_t stream);                                  \
+    cudaError_t launch_to_storage(const T* src, void* dst, int storage, int64_t n,         \
+                                  cudaStream_t stream);                                    \
+    cudaError_t launch_from_storage(const void* src, int storage, const double* undo,      \
+                                    T* dst, int64_t n, cudaStream_t stream);
 
 RLIC_DECLARE_LAUNCHERS(float)
 RLIC_DECLARE_LAUNCHERS(double)
+
+// Reduced-precision replay (lic_lowp.cu): `tex_in`/`tex_out` hold FP16 or
+// BF16 cells (`storage`), w32 the float kernel in natural order.
+cudaError_t launch_gather_lowp(int storage, const void* tex_in, const uint32_t* codes,
+                               const float* w32, int klen, const float* inv_scale,
+                               const Shape& sh, const LaunchConfig& lc, void* tex_out,
+                               cudaStream_t stream);
 
 #undef RLIC_DECLARE_LAUNCHERS
 

@@ -108,7 +108,7 @@ def test_sweep_and_replay_argument_errors(native) -> None:
 def test_block_shape_validation(native) -> None:
     assert native.rlic_set_block_shape(0, 4) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 64) == _native.RLIC_ERR_INVALID_ARGUMENT
-    assert native.rlic_set_block_shape(32, 8) == _native.RLIC_OK
+    assert native.rlic_set_block_shape(64, 4) == _native.RLIC_OK
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path) -> None:

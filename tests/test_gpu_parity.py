@@ -209,6 +209,22 @@ def test_degenerate_shapes_and_kernels(oracle, shape, klen) -> None:
         assert_bitwise(plain, want)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("klen", [9, 33, 65])
+def test_replay_interior_and_border_tiles(oracle, dtype, klen) -> None:
+    """Images large enough that replays run both from staged shared-memory
+    blocks (interior super-tiles) and from global memory (border ones)."""
+    rng = np.random.default_rng(klen)
+    ny, nx = 280, 344
+    u, v = _field(rng, ny, nx, dtype, "specials")
+    tex = rng.random((ny, nx)).astype(dtype)
+    k = rng.random(klen).astype(dtype)
+    for bnd, mode in (("periodic", "polarization"), ({"x": "closed", "y": "periodic"}, "velocity")):
+        want = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries=bnd, iterations=3,
+                               nthreads=oracle.env_threads())
+        assert_bitwise(capi_convolve(tex, u, v, k, mode, bnd, iterations=3), want)
+
+
 @pytest.mark.parametrize("iterations", [0, 1, 2, 3, 4])
 def test_iteration_counts(oracle, iterations) -> None:
     rng = np.random.default_rng(iterations)
