@@ -66,10 +66,12 @@ def parse_args() -> argparse.Namespace:
                    help="target CPU time of the oracle baseline sample")
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["fourier", "readme", "precision"], default="fourier",
+    p.add_argument("--workload", choices=["fourier", "readme", "precision", "adjoint"],
+                   default="fourier",
                    help="fourier: the headline 8192^2 float32 case (default); readme: the "
                         "reference's README case, 256^2 float64; precision: 8192^2 float64, "
-                        "K=129, 10 iterations, exact vs FP16/BF16 storage forms")
+                        "K=129, 10 iterations, exact vs FP16/BF16 storage forms; adjoint: "
+                        "1024^2 float32, K=33, 3 iterations, forward + backward")
     return p.parse_args()
 
 
@@ -621,6 +623,48 @@ def run_precision(args) -> None:
     }), flush=True)
 
 
+def run_adjoint(args) -> None:
+    """1024^2 float32 (README recipe, seed 4), K=33 triangle, periodic, n=3;
+    loss = sum(W * out), W ~ N(0, 1): forward + backward through
+    rlic_gb300.forms.convolve_autograd."""
+    import torch
+
+    from rlic_gb300.forms import convolve_autograd
+    from rlic_gb300.workloads import readme_case
+
+    n, klen, iters = 1024, 33, 3
+    c = readme_case(n=n, klen=klen, dtype=np.float32, seed=4)
+    dev = torch.device("cuda", 0)
+    t = {x: torch.from_numpy(np.ascontiguousarray(c[x])).to(dev) for x in ("texture", "u", "v", "kernel")}
+    W = torch.from_numpy(np.random.default_rng(4).normal(size=(n, n)).astype(np.float32)).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def fwd_bwd():
+        tex = t["texture"].detach().requires_grad_(True)
+        k = t["kernel"].detach().requires_grad_(True)
+        out = convolve_autograd(tex, t["u"], t["v"], kernel=k, boundaries="periodic",
+                                iterations=iters)
+        (out * W).sum().backward()
+        return tex.grad, k.grad
+
+    def fwd():
+        with torch.no_grad():
+            convolve_autograd(t["texture"], t["u"], t["v"], kernel=t["kernel"],
+                              boundaries="periodic", iterations=iters)
+
+    steps = max(args.steps, 20)
+    ms_fb = _time_calls(fwd_bwd, steps, args.warmup, stream)
+    ms_f = _time_calls(fwd, steps, args.warmup, stream)
+    samples = n * n * klen * iters
+    print(json.dumps({
+        "metric": METRIC, "unit": UNIT,
+        "workload": f"readme_recipe_{n}x{n}_f32_triangle{klen}_periodic_velocity_n{iters}_fwd_bwd",
+        "value": samples / (ms_fb / 1e3) / 1e9, "ms_per_step": ms_fb, "dtype": "f32",
+        "forward_only": {"ms": ms_f, "value": samples / (ms_f / 1e3) / 1e9},
+        "note": "value = forward samples per second of forward + backward (d/dtexture, d/dkernel)",
+    }), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist()
@@ -631,6 +675,8 @@ def main() -> None:
         run_readme(args)
     elif args.workload == "precision":
         run_precision(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gb300(args, dist)
 

@@ -136,6 +136,34 @@ RLIC_API int rlic_convolve_f64(const double *texture, const double *u, const dou
                       size_t workspace_bytes, void *stream, unsigned flags);
 
 /*
+ * Adjoint of one pass, for gradients (no counterpart in the reference).
+ *
+ * A pass is linear in the texture: out = A tex, with A[p, c] = sum of the
+ * kernel taps with which pixel p's streamlines sample cell c.  Given codes
+ * recorded by rlic_sweep_* (same ny, nx, klen):
+ *
+ * rlic_adjoint_*: y = A^T g (y is overwritten).  Accumulates with atomics,
+ *   so the summation order, and the last bits of y, vary from run to run.
+ * rlic_kernel_grad_*: dw[k] += sum_p g[p] * x[c_k(p)], the gradient of
+ *   <g, A x> with respect to kernel[k]; dw (klen doubles) is accumulated
+ *   into, so the caller zeroes it first.
+ *
+ * Device pointers, asynchronous on `stream`; `flags` must be 0.
+ */
+RLIC_API int rlic_adjoint_f32(const float *g, const void *codes, int64_t ny, int64_t nx,
+                              const float *kernel, int64_t klen, float *y, void *stream,
+                              unsigned flags);
+RLIC_API int rlic_adjoint_f64(const double *g, const void *codes, int64_t ny, int64_t nx,
+                              const double *kernel, int64_t klen, double *y, void *stream,
+                              unsigned flags);
+RLIC_API int rlic_kernel_grad_f32(const float *g, const float *x, const void *codes,
+                                  int64_t ny, int64_t nx, int64_t klen, double *dw,
+                                  void *stream, unsigned flags);
+RLIC_API int rlic_kernel_grad_f64(const double *g, const double *x, const void *codes,
+                                  int64_t ny, int64_t nx, int64_t klen, double *dw,
+                                  void *stream, unsigned flags);
+
+/*
  * Reduced-precision form of rlic_convolve_* (device pointers, asynchronous).
  *
  * Streamline cells come from a trace in the input dtype (the cell choices are

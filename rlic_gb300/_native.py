@@ -70,6 +70,10 @@ SIGNATURES: dict[str, tuple[list, object]] = {
                                 _I64, _INT, _P, _P, _SZ, _P, _U], _INT),
     "rlic_convolve_lowp_f64": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT, _INT,
                                 _I64, _INT, _P, _P, _SZ, _P, _U], _INT),
+    "rlic_adjoint_f32": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
+    "rlic_adjoint_f64": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
+    "rlic_kernel_grad_f32": ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _U], _INT),
+    "rlic_kernel_grad_f64": ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _U], _INT),
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),

@@ -462,6 +462,44 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
     return rc;
 }
 
+// --------------------------------------------------------------- adjoint --
+
+template <typename T>
+int adjoint_impl(const T* g, const void* codes, int64_t ny, int64_t nx, const T* kernel,
+                 int64_t klen, T* y, void* stream_, unsigned flags) {
+    g_last_error.clear();
+    int rc = check_shape(ny, nx, klen);
+    if (rc) return rc;
+    if (flags) return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes no flags");
+    if (!g || !kernel || !y || (!codes && klen > 1))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
+    const int bnd[4] = {0, 0, 0, 0};
+    RLIC_CUDA_TRY(rlic::launch_scatter(g, static_cast<const uint32_t*>(codes), kernel, int(klen),
+                                       make_shape(ny, nx, bnd), y,
+                                       static_cast<cudaStream_t>(stream_)));
+    return RLIC_OK;
+}
+
+template <typename T>
+int kernel_grad_impl(const T* g, const T* x, const void* codes, int64_t ny, int64_t nx,
+                     int64_t klen, double* dw, void* stream_, unsigned flags) {
+    g_last_error.clear();
+    int rc = check_shape(ny, nx, klen);
+    if (rc) return rc;
+    if (flags) return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes no flags");
+    if (!g || !x || !dw || (!codes && klen > 1))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
+    const int bnd[4] = {0, 0, 0, 0};
+    RLIC_CUDA_TRY(rlic::launch_kernel_grad(g, x, static_cast<const uint32_t*>(codes), int(klen),
+                                           make_shape(ny, nx, bnd), dw,
+                                           static_cast<cudaStream_t>(stream_)));
+    return RLIC_OK;
+}
+
 // ------------------------------------------------------- no-allocation path --
 //
 // Scratch of rlic_convolve_f32_noalloc, for callers that cannot allocate
@@ -641,6 +679,27 @@ int rlic_convolve_lowp_f64(const double* texture, const double* u, const double*
     return convolve_lowp_impl<double>(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left,
                                       bx_right, by_left, by_right, iterations, storage, out,
                                       workspace, workspace_bytes, stream, flags);
+}
+
+int rlic_adjoint_f32(const float* g, const void* codes, int64_t ny, int64_t nx,
+                     const float* kernel, int64_t klen, float* y, void* stream, unsigned flags) {
+    return adjoint_impl<float>(g, codes, ny, nx, kernel, klen, y, stream, flags);
+}
+
+int rlic_adjoint_f64(const double* g, const void* codes, int64_t ny, int64_t nx,
+                     const double* kernel, int64_t klen, double* y, void* stream,
+                     unsigned flags) {
+    return adjoint_impl<double>(g, codes, ny, nx, kernel, klen, y, stream, flags);
+}
+
+int rlic_kernel_grad_f32(const float* g, const float* x, const void* codes, int64_t ny,
+                         int64_t nx, int64_t klen, double* dw, void* stream, unsigned flags) {
+    return kernel_grad_impl<float>(g, x, codes, ny, nx, klen, dw, stream, flags);
+}
+
+int rlic_kernel_grad_f64(const double* g, const double* x, const void* codes, int64_t ny,
+                         int64_t nx, int64_t klen, double* dw, void* stream, unsigned flags) {
+    return kernel_grad_impl<double>(g, x, codes, ny, nx, klen, dw, stream, flags);
 }
 
 int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float* v,

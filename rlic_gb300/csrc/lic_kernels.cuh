@@ -273,6 +273,84 @@ __global__ void trace_cells_kernel(const typename Vec2<T>::type* __restrict__ uv
                                              [dst, nf](int s, int64_t c) { dst[nf + s] = c; });
 }
 
+// ------------------------------------------------------------ adjoint pass --
+//
+// One pass of the convolution is linear in the texture: out = A x with
+// A[p, c_k(p)] += kernel[k], c_k(p) the cell that pixel p's streamline samples
+// with tap k (c_kmid(p) = p).  Its transpose scatters: y[c_k(p)] += kernel[k]
+// * g[p].  Both kernels below walk the recorded step codes from every pixel,
+// so they see exactly the cells of the traced pass.
+
+// Calls f(k, cell) for every tap of pixel p, centre first, then the forward
+// taps ascending, then the backward taps descending.
+template <typename I, typename F>
+__device__ __forceinline__ void for_each_tap(I p, const uint32_t* __restrict__ codes,
+                                             const CodeLayout& cl, int klen, const I* table,
+                                             F f) {
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    f(kmid, p);
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t* words =
+            codes + (half ? size_t(cl.words_f) * size_t(cl.npix) : size_t(0)) + p;
+        const int count = half ? kmid : nf;
+        I cell = p;
+        for (int s = 0; s < count; ++s) {
+            const uint32_t wd = __ldg(words + size_t(s >> 3) * size_t(cl.npix));
+            const uint32_t code = (wd >> (4 * (s & 7))) & 15u;
+            if (code == kStop) break;
+            cell += table[code];
+            f(half ? kmid - 1 - s : kmid + 1 + s, cell);
+        }
+    }
+}
+
+// y = A^T g (y zeroed by the caller).  One thread per pixel, grid-stride.
+template <typename T, typename I>
+__global__ void __launch_bounds__(256)
+lic_scatter_kernel(const T* __restrict__ g, const uint32_t* __restrict__ codes,
+                   const T* __restrict__ kernel, int klen, Geometry<I> geo, CodeLayout cl,
+                   T* __restrict__ y) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* w = reinterpret_cast<T*>(smem_raw);
+    I* table = reinterpret_cast<I*>(smem_raw + sizeof(T) * size_t((klen + 1) & ~1));
+    for (int k = threadIdx.x; k < klen; k += blockDim.x) w[k] = kernel[k];
+    if (threadIdx.x == 0) fill_delta_table(table, geo.nx, geo.ny);
+    __syncthreads();
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < cl.npix; q += stride) {
+        const I p = I(q);
+        const T gp = g[p];
+        for_each_tap(p, codes, cl, klen, table,
+                     [&](int k, I cell) { atomicAdd(y + cell, mul_rn(w[k], gp)); });
+    }
+}
+
+// dw[k] += sum_p g[p] * x[c_k(p)]: the gradient of <g, A x> with respect to
+// kernel[k].  Per-CTA partial sums in shared memory, one global (float64)
+// atomic per tap per CTA.
+template <typename T, typename I>
+__global__ void __launch_bounds__(256)
+lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
+                       const uint32_t* __restrict__ codes, int klen, Geometry<I> geo,
+                       CodeLayout cl, double* __restrict__ dw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* acc = reinterpret_cast<T*>(smem_raw);
+    I* table = reinterpret_cast<I*>(smem_raw + sizeof(T) * size_t((klen + 1) & ~1));
+    for (int k = threadIdx.x; k < klen; k += blockDim.x) acc[k] = T(0);
+    if (threadIdx.x == 0) fill_delta_table(table, geo.nx, geo.ny);
+    __syncthreads();
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < cl.npix; q += stride) {
+        const I p = I(q);
+        const T gp = g[p];
+        for_each_tap(p, codes, cl, klen, table,
+                     [&](int k, I cell) { atomicAdd(acc + k, mul_rn(gp, __ldg(x + cell))); });
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < klen; k += blockDim.x) atomicAdd(dw + k, double(acc[k]));
+}
+
 // ------------------------------------------------ reduced-precision helpers --
 
 // Float copy of the kernel, 1/sum(|kernel|) as used by the reduced-precision
@@ -547,6 +625,48 @@ cudaError_t launch_from_storage_t(const void* src, int storage, const double* un
     return cudaGetLastError();
 }
 
+inline unsigned pixel_blocks(int64_t npix) {
+    int64_t blocks = (npix + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    return unsigned(blocks < 1 ? 1 : blocks);
+}
+
+template <typename T, typename I>
+cudaError_t launch_scatter_t(const T* g, const uint32_t* codes, const T* kernel, int klen,
+                             const Shape& sh, T* y, cudaStream_t stream) {
+    const auto geo = make_geometry<I>(sh);
+    const auto cl = make_code_layout(sh, klen);
+    const size_t smem = sizeof(T) * size_t((klen + 1) & ~1) + 16 * sizeof(I);
+    auto kfn = lic_scatter_kernel<T, I>;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(y, 0, size_t(cl.npix) * sizeof(T), stream);
+    if (e != cudaSuccess) return e;
+    kfn<<<pixel_blocks(cl.npix), 256, smem, stream>>>(g, codes, kernel, klen, geo, cl, y);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, typename I>
+cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, int klen,
+                                 const Shape& sh, double* dw, cudaStream_t stream) {
+    const auto geo = make_geometry<I>(sh);
+    const auto cl = make_code_layout(sh, klen);
+    const size_t smem = sizeof(T) * size_t((klen + 1) & ~1) + 16 * sizeof(I);
+    auto kfn = lic_kernel_grad_kernel<T, I>;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    kfn<<<pixel_blocks(cl.npix), 256, smem, stream>>>(g, x, codes, klen, geo, cl, dw);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // Definitions of the per-type overloads declared in lic_launch.h.
 #define RLIC_DEFINE_LAUNCHERS(T)                                                             \
     cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) { \
@@ -593,6 +713,18 @@ cudaError_t launch_from_storage_t(const void* src, int storage, const double* un
     cudaError_t launch_from_storage(const void* src, int storage, const double* undo, T* dst, \
                                     int64_t n, cudaStream_t stream) {                        \
         return launch_from_storage_t<T>(src, storage, undo, dst, n, stream);                 \
+    }                                                                                        \
+    cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel, int klen, \
+                               const Shape& sh, T* y, cudaStream_t stream) {                 \
+        return sh.small_index()                                                              \
+                   ? launch_scatter_t<T, int32_t>(g, codes, kernel, klen, sh, y, stream)     \
+                   : launch_scatter_t<T, int64_t>(g, codes, kernel, klen, sh, y, stream);    \
+    }                                                                                        \
+    cudaError_t launch_kernel_grad(const T* g, const T* x, const uint32_t* codes, int klen,  \
+                                   const Shape& sh, double* dw, cudaStream_t stream) {       \
+        return sh.small_index()                                                              \
+                   ? launch_kernel_grad_t<T, int32_t>(g, x, codes, klen, sh, dw, stream)     \
+                   : launch_kernel_grad_t<T, int64_t>(g, x, codes, klen, sh, dw, stream);    \
     }
 
 }  // namespace rlic

@@ -70,7 +70,12 @@ inline int64_t code_words_per_pixel(int64_t klen) {
     cudaError_t launch_to_storage(const T* src, void* dst, int storage, int64_t n,         \
                                   cudaStream_t stream);                                    \
     cudaError_t launch_from_storage(const void* src, int storage, const double* undo,      \
-                                    T* dst, int64_t n, cudaStream_t stream);
+                                    T* dst, int64_t n, cudaStream_t stream);               \
+    cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel,         \
+                               int klen, const Shape& sh, T* y, cudaStream_t stream);      \
+    cudaError_t launch_kernel_grad(const T* g, const T* x, const uint32_t* codes,          \
+                                   int klen, const Shape& sh, double* dw,                  \
+                                   cudaStream_t stream);
 
 RLIC_DECLARE_LAUNCHERS(float)
 RLIC_DECLARE_LAUNCHERS(double)

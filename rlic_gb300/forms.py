@@ -1,5 +1,12 @@
 """Forms beyond the drop-in ``convolve``.
 
+``convolve_autograd``: the differentiable form, a ``torch.autograd.Function``
+whose forward is bit-identical to ``convolve`` and whose backward runs the
+adjoint on the GPU: the transpose of every pass scatters the incoming
+gradient back along the same recorded streamlines (d loss / d texture), and
+a per-tap reduction gives d loss / d kernel.  u and v are not
+differentiable: the streamline cells are discrete choices.
+
 ``convolve_lowp``: the reduced-precision form.  Streamline cells are traced
 in the input dtype (float64 inputs keep a float64 advance), then the texture
 and every buffer between passes are stored as FP16 or BF16 and each pass
@@ -13,7 +20,7 @@ and validate their inputs with the same rules and messages.
 
 from __future__ import annotations
 
-__all__ = ["convolve_lowp"]
+__all__ = ["convolve_autograd", "convolve_lowp"]
 
 import ctypes
 from typing import Any
@@ -93,3 +100,119 @@ def convolve_lowp(
     if use_torch:
         return out
     return out.cpu().numpy()
+
+
+# ------------------------------------------------------------ differentiable --
+
+def _launch(fn, *args) -> None:
+    _native.check(fn(*args))
+
+
+class _ConvolveFunction:
+    """Namespace for the torch.autograd.Function (built lazily: torch import)."""
+
+    cls = None
+
+    @classmethod
+    def get(cls):
+        if cls.cls is not None:
+            return cls.cls
+        import torch
+
+        class ConvolveFunction(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, texture, kernel, u, v, uv_code, bcodes, iterations):
+                lib = _native.lib()
+                f32 = texture.dtype == torch.float32
+                sfx = "f32" if f32 else "f64"
+                ny, nx = texture.shape
+                klen = kernel.shape[0]
+                dev = texture.device
+                stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+                uv = torch.empty((ny, nx, 2), dtype=texture.dtype, device=dev)
+                codes = torch.empty(max(lib.rlic_path_code_bytes(ny, nx, klen), 4),
+                                    dtype=torch.uint8, device=dev)
+                _launch(getattr(lib, f"rlic_pack_field_{sfx}"), u.data_ptr(), v.data_ptr(), ny,
+                        nx, uv.data_ptr(), stream)
+                xs = [texture]
+                first = torch.empty_like(texture)
+                _launch(getattr(lib, f"rlic_sweep_{sfx}"), texture.data_ptr(), uv.data_ptr(), ny,
+                        nx, kernel.data_ptr(), klen, uv_code, *bcodes, first.data_ptr(),
+                        codes.data_ptr(), stream, 0)
+                xs.append(first)
+                for _ in range(1, iterations):
+                    nxt = torch.empty_like(texture)
+                    _launch(getattr(lib, f"rlic_replay_{sfx}"), xs[-1].data_ptr(),
+                            codes.data_ptr(), ny, nx, kernel.data_ptr(), klen, nxt.data_ptr(),
+                            stream, 0)
+                    xs.append(nxt)
+                ctx.save_for_backward(kernel, codes, *xs[:-1])
+                ctx.iterations = iterations
+                return xs[-1]
+
+            @staticmethod
+            def backward(ctx, grad_out):
+                lib = _native.lib()
+                kernel, codes, *xs = ctx.saved_tensors
+                n = ctx.iterations
+                f32 = grad_out.dtype == torch.float32
+                sfx = "f32" if f32 else "f64"
+                ny, nx = grad_out.shape
+                klen = kernel.shape[0]
+                dev = grad_out.device
+                stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+                need_tex, need_k = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+                g = grad_out.contiguous()
+                dw = torch.zeros(klen, dtype=torch.float64, device=dev)
+                for m in range(n):
+                    if need_k:
+                        _launch(getattr(lib, f"rlic_kernel_grad_{sfx}"), g.data_ptr(),
+                                xs[n - 1 - m].data_ptr(), codes.data_ptr(), ny, nx, klen,
+                                dw.data_ptr(), stream, 0)
+                    if need_tex or m < n - 1:
+                        y = torch.empty_like(g)
+                        _launch(getattr(lib, f"rlic_adjoint_{sfx}"), g.data_ptr(),
+                                codes.data_ptr(), ny, nx, kernel.data_ptr(), klen, y.data_ptr(),
+                                stream, 0)
+                        g = y
+                grad_tex = g if need_tex else None
+                grad_k = dw.to(kernel.dtype) if need_k else None
+                return grad_tex, grad_k, None, None, None, None, None
+
+        cls.cls = ConvolveFunction
+        return ConvolveFunction
+
+
+def convolve_autograd(
+    texture: Any,
+    /,
+    u: Any,
+    v: Any,
+    *,
+    kernel: Any,
+    uv_mode: str = "velocity",
+    boundaries: Any = "closed",
+    iterations: int = 1,
+) -> Any:
+    """Differentiable ``convolve`` on torch CUDA tensors.
+
+    Same arguments, validation and (bit-identical) result as ``convolve``;
+    gradients flow to ``texture`` and ``kernel``.  d loss / d texture
+    accumulates with atomics, so its last bits vary from run to run.
+    """
+    import torch
+
+    if not _is_torch(texture):
+        raise TypeError("convolve_autograd takes torch CUDA tensors")
+    _, bs = _validated(texture, u, v, kernel, uv_mode, boundaries, iterations)
+    if iterations == 0:
+        return texture.clone()
+    dev = texture.device
+    if dev.type != "cuda":
+        raise ValueError("convolve_autograd takes CUDA tensors")
+    u_c, v_c = (a.detach().to(device=dev).contiguous() for a in (u, v))
+    with torch.cuda.device(dev):
+        return _ConvolveFunction.get().apply(
+            texture.contiguous(), kernel.to(device=dev).contiguous(), u_c, v_c,
+            _native.UV_MODE_CODES[uv_mode], bs.codes(), iterations,
+        )
