@@ -66,12 +66,14 @@ def parse_args() -> argparse.Namespace:
                    help="target CPU time of the oracle baseline sample")
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["fourier", "readme", "precision", "adjoint"],
+    p.add_argument("--workload",
+                   choices=["fourier", "readme", "precision", "adjoint", "batched"],
                    default="fourier",
                    help="fourier: the headline 8192^2 float32 case (default); readme: the "
                         "reference's README case, 256^2 float64; precision: 8192^2 float64, "
                         "K=129, 10 iterations, exact vs FP16/BF16 storage forms; adjoint: "
-                        "1024^2 float32, K=33, 3 iterations, forward + backward")
+                        "1024^2 float32, K=33, 3 iterations, forward + backward; batched: 64 "
+                        "instances of sides 256-4096, K 17-129, 1-10 iterations")
     return p.parse_args()
 
 
@@ -665,6 +667,74 @@ def run_adjoint(args) -> None:
     }), flush=True)
 
 
+def run_batched(args) -> None:
+    """64 instances (rlic_gb300.workloads.batch_case, seed 3): one batched call
+    (and its CUDA-graph replay) against 64 sequential rlic_convolve_f32 calls."""
+    import torch
+
+    from rlic_gb300 import _native
+    from rlic_gb300.batch import BatchPlan, autotune_tiles
+    from rlic_gb300.workloads import batch_case
+
+    items = batch_case(count=64, seed=3)
+    dev = items[0]["texture"].device
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    lib = _native.lib()
+    t0 = time.perf_counter()
+    choice = autotune_tiles(items)
+    tune_s = time.perf_counter() - t0
+    plan = BatchPlan(items)
+    samples = plan.samples()
+    steps = max(3, min(args.steps, 10))
+    ms_batch = _time_calls(plan.run, steps, args.warmup, stream)
+    plan.capture()
+    ms_graph = _time_calls(plan.replay, steps, args.warmup, stream)
+
+    seq = []
+    for it, t in zip(items, plan.inputs):
+        ny, nx = t["texture"].shape
+        klen = t["kernel"].shape[0]
+        from rlic_gb300._boundaries import BoundarySet
+
+        bc = BoundarySet.from_spec(it["boundaries"]).codes()
+        out = torch.empty_like(t["texture"])
+        seq.append((t, ny, nx, klen, it["iterations"], _native.UV_MODE_CODES[it["uv_mode"]], bc, out))
+    wsmax = max(lib.rlic_workspace_bytes(ny, nx, klen, n, 4, 0)
+                for _, ny, nx, klen, n, _, _, _ in seq)
+    ws = torch.empty(wsmax, dtype=torch.uint8, device=dev)
+
+    def sequential(flags):
+        def go():
+            for t, ny, nx, klen, n, mode, bc, out in seq:
+                _native.check(lib.rlic_convolve_f32(
+                    t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), ny, nx,
+                    t["kernel"].data_ptr(), klen, mode, *bc, n, out.data_ptr(), ws.data_ptr(),
+                    wsmax, sp, flags))
+        return go
+
+    ms_seq = _time_calls(sequential(0), steps, args.warmup, stream)
+    ms_seq_plain = _time_calls(sequential(_native.RLIC_FLAG_NO_PATH_CACHE), 2, 1, stream)
+    for (_, _, _, _, _, _, _, out), got in zip(seq, plan.outputs):
+        assert torch.equal(out, got), "batched result differs from the sequential calls"
+
+    def gs(ms):
+        return samples / (ms / 1e3) / 1e9
+
+    print(json.dumps({
+        "metric": METRIC, "unit": UNIT, "workload": "batch_64_instances_seed3",
+        "value": gs(ms_graph), "dtype": "f32", "samples_per_step": samples,
+        "pixels": int(sum(int(i["texture"].numel()) for i in items)),
+        "forms": {
+            "batched_graph_replay": {"ms": ms_graph, "value": gs(ms_graph)},
+            "batched_call": {"ms": ms_batch, "value": gs(ms_batch)},
+            "sequential_path_cache_calls": {"ms": ms_seq, "value": gs(ms_seq)},
+            "sequential_plain_calls": {"ms": ms_seq_plain, "value": gs(ms_seq_plain)},
+        },
+        "autotune": {"seconds": tune_s, "choices": {str(k): v for k, v in choice.items()}},
+    }), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist()
@@ -677,6 +747,8 @@ def main() -> None:
         run_precision(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_gb300(args, dist)
 

@@ -136,6 +136,39 @@ RLIC_API int rlic_convolve_f64(const double *texture, const double *u, const dou
                       size_t workspace_bytes, void *stream, unsigned flags);
 
 /*
+ * Batched form (float32, default arithmetic): many independent convolutions
+ * of uneven sizes, kernel lengths, boundaries, uv modes and iteration counts
+ * in one call.  Results are bit-identical to one rlic_convolve_f32 call per
+ * item.  No counterpart in the reference.
+ *
+ * The call launches one kernel that packs every item's field, then one per
+ * pass level: level 1 traces every item (recording its path cache when it has
+ * two or more iterations), level L replays the items with at least L
+ * iterations; each launch spreads the tiles of all its items over the whole
+ * GPU.  tile_x (tile_y = 256 / tile_x) sets an item's CTA tile shape (0: 64).
+ *
+ * The per-item tables live at the start of the workspace
+ * (rlic_batch_workspace_bytes_f32 bytes, 256-byte aligned).  With
+ * RLIC_FLAG_BATCH_PREPARED the call assumes the workspace already holds the
+ * tables of the same `items` (written by an earlier call) and issues kernel
+ * launches and memsets only, with no host-to-device copy.  All pointers are
+ * device memory; asynchronous on `stream`.  Limits: at most 1024 items, each
+ * below 2^31 pixels, kernels of at most 1025 taps.
+ */
+typedef struct rlic_batch_item_f32 {
+    const float *texture, *u, *v, *kernel; /* device, C-order ny x nx; klen taps */
+    float *out;                            /* device, ny x nx */
+    int64_t ny, nx, klen, iterations;
+    int uv_mode, bx_left, bx_right, by_left, by_right;
+    int tile_x;
+} rlic_batch_item_f32;
+#define RLIC_FLAG_BATCH_PREPARED 0x10u
+RLIC_API size_t rlic_batch_workspace_bytes_f32(const rlic_batch_item_f32 *items, int count);
+RLIC_API int rlic_convolve_batch_f32(const rlic_batch_item_f32 *items, int count,
+                                     void *workspace, size_t workspace_bytes, void *stream,
+                                     unsigned flags);
+
+/*
  * Adjoint of one pass, for gradients (no counterpart in the reference).
  *
  * A pass is linear in the texture: out = A tex, with A[p, c] = sum of the

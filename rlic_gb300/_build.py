@@ -42,7 +42,13 @@ NVCC_FLAGS = [
     "-warn-spills",
 ]
 
-SOURCES = ["lic_capi.cu", "lic_kernels_f32.cu", "lic_kernels_f64.cu", "lic_lowp.cu"]
+SOURCES = [
+    "lic_capi.cu",
+    "lic_kernels_f32.cu",
+    "lic_kernels_f64.cu",
+    "lic_lowp.cu",
+    "lic_batch.cu",
+]
 
 
 def nvcc_path() -> str:

@@ -74,11 +74,29 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_adjoint_f64": ([_P, _P, _I64, _I64, _P, _I64, _P, _P, _U], _INT),
     "rlic_kernel_grad_f32": ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _U], _INT),
     "rlic_kernel_grad_f64": ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _U], _INT),
+    "rlic_batch_workspace_bytes_f32": ([_P, _INT], _SZ),
+    "rlic_convolve_batch_f32": ([_P, _INT, _P, _SZ, _P, _U], _INT),
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
 }
+
+
+class BatchItemF32(ctypes.Structure):
+    """rlic_batch_item_f32 (include/rlic_gb300.h)."""
+
+    _fields_ = [
+        ("texture", ctypes.c_void_p), ("u", ctypes.c_void_p), ("v", ctypes.c_void_p),
+        ("kernel", ctypes.c_void_p), ("out", ctypes.c_void_p),
+        ("ny", ctypes.c_int64), ("nx", ctypes.c_int64), ("klen", ctypes.c_int64),
+        ("iterations", ctypes.c_int64),
+        ("uv_mode", ctypes.c_int), ("bx_left", ctypes.c_int), ("bx_right", ctypes.c_int),
+        ("by_left", ctypes.c_int), ("by_right", ctypes.c_int), ("tile_x", ctypes.c_int),
+    ]
+
+
+RLIC_FLAG_BATCH_PREPARED = 0x10
 
 
 class NativeLibraryError(RuntimeError):

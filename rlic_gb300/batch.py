@@ -1,0 +1,164 @@
+"""The batched form: many independent float32 convolutions in one call.
+
+``BatchPlan`` takes a list of items (dicts with the arguments of
+``convolve``: ``texture``, ``u``, ``v``, ``kernel`` as float32 CUDA tensors,
+plus ``uv_mode``, ``boundaries``, ``iterations`` and optionally ``tile_x``),
+validates every item with the rules and messages of ``convolve``, and
+preallocates the outputs and one workspace.  ``run()`` launches one kernel
+that packs every field, then one kernel per pass level over all items
+(rlic_convolve_batch_f32).  ``capture()`` records a run into a CUDA graph so
+that ``replay()`` re-runs the whole batch with a single graph launch; write
+new textures into the plan's input tensors in place between replays.
+
+``autotune_tiles`` picks each item's CTA tile shape by timing the candidates
+on that item, once per distinct (side bucket, kernel length, uv mode).
+Results are bit-identical to one ``convolve`` call per item, whatever the
+tile shapes.
+"""
+
+from __future__ import annotations
+
+__all__ = ["BatchPlan", "autotune_tiles", "convolve_batch"]
+
+import ctypes
+import math
+from typing import Any
+
+from rlic_gb300 import _native
+from rlic_gb300._lib import _collect_problems, _Ops
+
+TILE_CANDIDATES = (64, 32, 16)
+
+
+def _validate_item(k: int, item: dict) -> tuple:
+    import torch
+
+    tex, u, v, kern = (item[x] for x in ("texture", "u", "v", "kernel"))
+    if not all(isinstance(a, torch.Tensor) for a in (tex, u, v, kern)):
+        raise TypeError(f"batch item {k}: texture, u, v and kernel must be torch tensors")
+    problems, bs = _collect_problems(
+        _Ops(True), tex, u, v, kern, item.get("uv_mode", "velocity"),
+        item.get("boundaries", "closed"), item.get("iterations", 1),
+    )
+    if len(problems) == 1:
+        raise problems[0]
+    if problems:
+        raise ExceptionGroup(f"Invalid inputs were received (batch item {k}).", problems)
+    if tex.dtype != torch.float32 or not tex.is_cuda:
+        raise TypeError(f"batch item {k}: the batched form takes float32 CUDA tensors")
+    return bs
+
+
+class BatchPlan:
+    """Preallocated batch of convolutions (see the module docstring)."""
+
+    def __init__(self, items: list[dict]) -> None:
+        import torch
+
+        if not items:
+            raise ValueError("empty batch")
+        self.lib = _native.lib()
+        self.device = items[0]["texture"].device
+        self.inputs: list[dict] = []
+        self.outputs: list[Any] = []
+        arr = (_native.BatchItemF32 * len(items))()
+        for k, item in enumerate(items):
+            bs = _validate_item(k, item)
+            t = {x: item[x].to(device=self.device).contiguous() for x in ("texture", "u", "v", "kernel")}
+            out = torch.empty_like(t["texture"])
+            self.inputs.append(t)
+            self.outputs.append(out)
+            ny, nx = t["texture"].shape
+            xl, xr, yl, yr = bs.codes()
+            arr[k] = _native.BatchItemF32(
+                t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(),
+                t["kernel"].data_ptr(), out.data_ptr(), ny, nx, t["kernel"].shape[0],
+                int(item.get("iterations", 1)),
+                _native.UV_MODE_CODES[item.get("uv_mode", "velocity")], xl, xr, yl, yr,
+                int(item.get("tile_x", 0)),
+            )
+        self.items = arr
+        self.count = len(items)
+        nbytes = self.lib.rlic_batch_workspace_bytes_f32(self.items, self.count)
+        self.workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
+        self.nbytes = nbytes
+        self.prepared = False
+        self.graph = None
+
+    def samples(self) -> int:
+        return sum(int(it.ny * it.nx * it.klen * it.iterations) for it in self.items)
+
+    def run(self) -> list:
+        """Launch the batch on the current stream; returns the output tensors."""
+        import torch
+
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        flags = _native.RLIC_FLAG_BATCH_PREPARED if self.prepared else 0
+        _native.check(self.lib.rlic_convolve_batch_f32(
+            self.items, self.count, self.workspace.data_ptr(), self.nbytes, stream, flags))
+        self.prepared = True
+        return self.outputs
+
+    def capture(self) -> None:
+        """Record one prepared run into a CUDA graph (replay() re-runs it)."""
+        import torch
+
+        if not self.prepared:
+            self.run()
+            torch.cuda.synchronize(self.device)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(side), torch.cuda.graph(graph, stream=side):
+            self.run()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        self.graph = graph
+
+    def replay(self) -> list:
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        self.graph.replay()
+        return self.outputs
+
+
+def convolve_batch(items: list[dict]) -> list:
+    """One-shot batch: validate, run, and return the outputs."""
+    return BatchPlan(items).run()
+
+
+def _bucket(item: dict) -> tuple:
+    ny, nx = item["texture"].shape
+    return (round(math.log2(max(ny * nx, 1)) / 2), int(item["kernel"].shape[0]),
+            item.get("uv_mode", "velocity"))
+
+
+def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
+                   repeats: int = 2) -> dict:
+    """Sets item["tile_x"] to the fastest candidate for each distinct bucket.
+
+    Each bucket is timed on its first item as a one-item batch.  Returns the
+    choice per bucket.
+    """
+    import torch
+
+    choice: dict = {}
+    for item in items:
+        key = _bucket(item)
+        if key not in choice:
+            best, best_ms = candidates[0], float("inf")
+            for tx in candidates:
+                plan = BatchPlan([{**item, "tile_x": tx}])
+                plan.run()
+                torch.cuda.synchronize(plan.device)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for _ in range(repeats):
+                    plan.run()
+                b.record()
+                torch.cuda.synchronize(plan.device)
+                ms = a.elapsed_time(b) / repeats
+                if ms < best_ms:
+                    best, best_ms = tx, ms
+            choice[key] = best
+        item["tile_x"] = choice[key]
+    return choice

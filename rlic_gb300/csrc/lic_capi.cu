@@ -22,11 +22,14 @@
 //               (lic_gather_kernel).  Streamline cells do not depend on the
 //               texture, so both forms give identical results.
 #include "../../include/rlic_gb300.h"
+#include "lic_batch.h"
 #include "lic_launch.h"
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace rlic {
 
@@ -500,6 +503,146 @@ int kernel_grad_impl(const T* g, const T* x, const void* codes, int64_t ny, int6
     return RLIC_OK;
 }
 
+// ------------------------------------------------------------ batched form --
+
+struct BatchLayout {
+    size_t insts, levels, total;
+    std::vector<size_t> uv, tmp, codes;  // per item
+    int max_iterations;
+};
+
+bool batch_tile_ok(int tx) { return tx == 8 || tx == 16 || tx == 32 || tx == 64 || tx == 128 || tx == 256; }
+
+int batch_check(const rlic_batch_item_f32* items, int count) {
+    if (count <= 0 || !items) return fail(RLIC_ERR_INVALID_ARGUMENT, "empty batch");
+    if (count > 1024) return fail(RLIC_ERR_INVALID_ARGUMENT, "at most 1024 items per batch");
+    for (int k = 0; k < count; ++k) {
+        const auto& it = items[k];
+        const int bnd[4] = {it.bx_left, it.bx_right, it.by_left, it.by_right};
+        int rc = check_common(it.ny, it.nx, it.klen, it.uv_mode, bnd, 0);
+        if (rc) return fail(rc, "item " + std::to_string(k) + ": " + g_last_error);
+        if (it.ny * it.nx >= (int64_t(1) << 31) - 1)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": image too large for a batch");
+        if (it.klen > 2 * rlic::kBatchMaxHalf + 1)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": kernel longer than 1025 taps");
+        if (it.iterations < 0 || it.iterations > 4096)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": iterations must be in [0, 4096]");
+        if (it.tile_x != 0 && !batch_tile_ok(it.tile_x))
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": tile_x must be 0 or a power of two in [8, 256]");
+        if (!it.texture || !it.u || !it.v || !it.kernel || !it.out)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": null array pointer");
+    }
+    return RLIC_OK;
+}
+
+BatchLayout batch_layout(const rlic_batch_item_f32* items, int count) {
+    BatchLayout L;
+    size_t off = 0;
+    L.insts = off;
+    off += align_up(size_t(count) * sizeof(rlic::BatchInstance));
+    L.max_iterations = 0;
+    for (int k = 0; k < count; ++k) L.max_iterations = std::max<int>(L.max_iterations, int(items[k].iterations));
+    L.levels = off;
+    off += align_up(size_t(std::max(L.max_iterations, 1)) * size_t(count) * (sizeof(int64_t) + sizeof(int)));
+    for (int k = 0; k < count; ++k) {
+        const auto& it = items[k];
+        const size_t n = size_t(it.ny) * size_t(it.nx);
+        L.uv.push_back(off);
+        off += align_up(2 * n * sizeof(float));
+        L.tmp.push_back(off);
+        if (it.iterations >= 2) off += align_up(n * sizeof(float));
+        L.codes.push_back(off);
+        if (it.iterations >= 2 && it.klen > 1) off += align_up(code_bytes(it.ny, it.nx, it.klen));
+    }
+    L.total = off;
+    return L;
+}
+
+int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* workspace,
+                       size_t workspace_bytes_, void* stream_, unsigned flags) {
+    g_last_error.clear();
+    int rc = batch_check(items, count);
+    if (rc) return rc;
+    if (flags & ~unsigned(RLIC_FLAG_BATCH_PREPARED))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes RLIC_FLAG_BATCH_PREPARED only");
+    if (!workspace) return fail(RLIC_ERR_INVALID_ARGUMENT, "the batched form needs a workspace");
+    const BatchLayout L = batch_layout(items, count);
+    if (workspace_bytes_ < L.total)
+        return fail(RLIC_ERR_WORKSPACE_TOO_SMALL, "workspace smaller than rlic_batch_workspace_bytes_f32()");
+    if (reinterpret_cast<uintptr_t>(workspace) % kAlign != 0)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    unsigned char* ws = static_cast<unsigned char*>(workspace);
+    auto* dev_insts = reinterpret_cast<rlic::BatchInstance*>(ws + L.insts);
+    auto* dev_starts = reinterpret_cast<int64_t*>(ws + L.levels);
+    auto* dev_index = reinterpret_cast<int*>(ws + L.levels + size_t(std::max(L.max_iterations, 1)) *
+                                                                 size_t(count) * sizeof(int64_t));
+    // host tables: instances, then for every level the participating instances
+    std::vector<rlic::BatchInstance> insts(count);
+    std::vector<int64_t> starts(size_t(std::max(L.max_iterations, 1)) * count, 0);
+    std::vector<int> index(starts.size(), 0);
+    std::vector<rlic::BatchLevel> levels(L.max_iterations + 1);
+    int64_t max_pixels = 0;
+    for (int k = 0; k < count; ++k) {
+        const auto& it = items[k];
+        auto& b = insts[k];
+        b.texture = it.texture;
+        b.u = it.u;
+        b.v = it.v;
+        b.kernel = it.kernel;
+        b.out = it.out;
+        b.tmp = reinterpret_cast<float*>(ws + L.tmp[k]);
+        b.uv = ws + L.uv[k];
+        b.codes = reinterpret_cast<uint32_t*>(ws + L.codes[k]);
+        b.ny = int(it.ny);
+        b.nx = int(it.nx);
+        b.klen = int(it.klen);
+        b.iterations = int(it.iterations);
+        b.pol = it.uv_mode == RLIC_UV_POLARIZATION;
+        b.bnd[0] = it.bx_left;
+        b.bnd[1] = it.bx_right;
+        b.bnd[2] = it.by_left;
+        b.bnd[3] = it.by_right;
+        b.tile_x = it.tile_x ? it.tile_x : 64;
+        b.tile_y = 256 / b.tile_x;
+        b.tiles_x = int((it.nx + b.tile_x - 1) / b.tile_x);
+        b.ntiles = b.tiles_x * int((it.ny + b.tile_y - 1) / b.tile_y);
+        max_pixels = std::max<int64_t>(max_pixels, it.ny * it.nx);
+    }
+    for (int level = 1; level <= L.max_iterations; ++level) {
+        const size_t base = size_t(level - 1) * size_t(count);
+        int m = 0;
+        int64_t tiles = 0;
+        for (int k = 0; k < count; ++k) {
+            if (insts[k].iterations < level) continue;
+            starts[base + m] = tiles;
+            index[base + m] = k;
+            tiles += insts[k].ntiles;
+            ++m;
+        }
+        levels[level] = rlic::BatchLevel{dev_starts + base, dev_index + base, m, tiles};
+    }
+    if (!(flags & RLIC_FLAG_BATCH_PREPARED)) {
+        // pageable copies: the call returns once the host tables are staged
+        RLIC_CUDA_TRY(cudaMemcpyAsync(dev_insts, insts.data(), insts.size() * sizeof(insts[0]),
+                                      cudaMemcpyHostToDevice, stream));
+        RLIC_CUDA_TRY(cudaMemcpyAsync(dev_starts, starts.data(), starts.size() * sizeof(int64_t),
+                                      cudaMemcpyHostToDevice, stream));
+        RLIC_CUDA_TRY(cudaMemcpyAsync(dev_index, index.data(), index.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice, stream));
+    }
+    // iterations == 0 items: zeros, as rlic_convolve_f32
+    for (int k = 0; k < count; ++k)
+        if (items[k].iterations == 0)
+            RLIC_CUDA_TRY(cudaMemsetAsync(items[k].out, 0,
+                                          size_t(items[k].ny) * size_t(items[k].nx) * 4, stream));
+    if (L.max_iterations == 0) return RLIC_OK;
+    RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
+    for (int level = 1; level <= L.max_iterations; ++level)
+        RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));
+    return RLIC_OK;
+}
+
 // ------------------------------------------------------- no-allocation path --
 //
 // Scratch of rlic_convolve_f32_noalloc, for callers that cannot allocate
@@ -700,6 +843,16 @@ int rlic_kernel_grad_f32(const float* g, const float* x, const void* codes, int6
 int rlic_kernel_grad_f64(const double* g, const double* x, const void* codes, int64_t ny,
                          int64_t nx, int64_t klen, double* dw, void* stream, unsigned flags) {
     return kernel_grad_impl<double>(g, x, codes, ny, nx, klen, dw, stream, flags);
+}
+
+size_t rlic_batch_workspace_bytes_f32(const rlic_batch_item_f32* items, int count) {
+    if (!items || count <= 0) return 0;
+    return batch_layout(items, count).total;
+}
+
+int rlic_convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* workspace,
+                            size_t workspace_bytes, void* stream, unsigned flags) {
+    return convolve_batch_f32(items, count, workspace, workspace_bytes, stream, flags);
 }
 
 int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float* v,

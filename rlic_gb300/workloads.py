@@ -118,6 +118,41 @@ def fourier_vortex_case(
     )
 
 
+def batch_case(count: int = 64, seed: int = 3, device: str = "cuda", min_side: int = 256,
+               max_side: int = 4096) -> list[dict]:
+    """Batched workload: `count` independent float32 instances.
+
+    Square sides log-uniform in [min_side, max_side] (seed 3), fields and
+    textures as in ``readme_case`` with per-instance seeds, kernel lengths
+    uniform over the odd values in [17, 129] (triangle or Hann), boundaries
+    drawn per axis from {closed, periodic}, uv_mode drawn per instance,
+    iterations uniform in [1, 10].  Returns dicts of ``convolve`` arguments
+    with torch tensors on `device`.
+    """
+    import torch
+
+    rng = np.random.default_rng(seed)
+    items = []
+    for k in range(count):
+        side = int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side)))))
+        klen = int(rng.choice(np.arange(17, 130, 2)))
+        hann = bool(rng.integers(0, 2))
+        bx = ["closed", "periodic"][int(rng.integers(0, 2))]
+        by = ["closed", "periodic"][int(rng.integers(0, 2))]
+        uv_mode = ["velocity", "polarization"][int(rng.integers(0, 2))]
+        iterations = int(rng.integers(1, 11))
+        c = readme_case(n=side, klen=klen, dtype=np.float32, seed=seed * 1000 + k)
+        kernel = np.hanning(klen).astype(np.float32) if hann else c["kernel"]
+        items.append(dict(
+            texture=torch.from_numpy(c["texture"]).to(device),
+            u=torch.from_numpy(np.ascontiguousarray(c["u"])).to(device),
+            v=torch.from_numpy(np.ascontiguousarray(c["v"])).to(device),
+            kernel=torch.from_numpy(kernel).to(device), uv_mode=uv_mode,
+            boundaries={"x": bx, "y": by}, iterations=iterations,
+        ))
+    return items
+
+
 def samples(case: dict) -> int:
     """Kernel-weighted texture reads of a case: H * W * K * iterations."""
     ny, nx = case["texture"].shape

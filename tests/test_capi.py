@@ -105,6 +105,23 @@ def test_sweep_and_replay_argument_errors(native) -> None:
     assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
 
 
+def test_batch_argument_errors(native) -> None:
+    assert native.rlic_convolve_batch_f32(None, 0, None, 0, None, 0) == _native.RLIC_ERR_INVALID_ARGUMENT
+    items = (_native.BatchItemF32 * 1)()
+    items[0] = _native.BatchItemF32(1, 1, 1, 1, 1, 8, 8, 5, 1, 0, 0, 0, 0, 0, 24)
+    rc = native.rlic_convolve_batch_f32(items, 1, 256, 1 << 20, None, 0)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert "tile_x" in native.rlic_last_error().decode()
+    items[0] = _native.BatchItemF32(1, 1, 1, 1, 1, 8, 8, 2049, 1, 0, 0, 0, 0, 0, 0)
+    rc = native.rlic_convolve_batch_f32(items, 1, 256, 1 << 20, None, 0)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert "1025 taps" in native.rlic_last_error().decode()
+    items[0] = _native.BatchItemF32(1, 1, 1, 1, 1, 8, 8, 5, 1, 0, 0, 0, 0, 0, 0)
+    assert native.rlic_batch_workspace_bytes_f32(items, 1) > 0
+    rc = native.rlic_convolve_batch_f32(items, 1, 256, 16, None, 0)
+    assert rc == _native.RLIC_ERR_WORKSPACE_TOO_SMALL
+
+
 def test_block_shape_validation(native) -> None:
     assert native.rlic_set_block_shape(0, 4) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 64) == _native.RLIC_ERR_INVALID_ARGUMENT
