@@ -53,6 +53,7 @@ extern "C" {
 #define RLIC_ERR_CUDA 2
 #define RLIC_ERR_OUT_OF_MEMORY 3
 #define RLIC_ERR_WORKSPACE_TOO_SMALL 4
+#define RLIC_ERR_NEGATIVE_TEXTURE 5
 
 /* uv_mode: src/lib.rs:14-27 ("velocity" / "polarization") */
 #define RLIC_UV_VELOCITY 0
@@ -67,6 +68,7 @@ extern "C" {
 #define RLIC_FLAG_NO_FMA 0x2u        /* reference built without feature `fma`       */
 #define RLIC_FLAG_NO_BRANCHLESS 0x4u /* reference built without feature `branchless` */
 #define RLIC_FLAG_NO_PATH_CACHE 0x8u /* trace every streamline in every pass          */
+#define RLIC_FLAG_CHECK_TEXTURE 0x20u /* with HOST_MEMORY: fail if texture has x < 0   */
 
 /* Library version string. */
 RLIC_API const char *rlic_version(void);
@@ -118,6 +120,14 @@ RLIC_API size_t rlic_path_code_bytes(int64_t ny, int64_t nx, int64_t klen);
  *                   (the path of a pixel depends on u, v and the kernel
  *                   length only); RLIC_FLAG_NO_PATH_CACHE traces every pass.
  *                   Both give identical results.
+ *                   RLIC_FLAG_CHECK_TEXTURE (with RLIC_FLAG_HOST_MEMORY) tests
+ *                   the texture for elements below zero on the device, as
+ *                   src/rlic/_lib.py:174-179 does on the host, and returns
+ *                   RLIC_ERR_NEGATIVE_TEXTURE (`out` then undefined).
+ *                   With RLIC_FLAG_HOST_MEMORY on a device that can access
+ *                   pageable host memory (Grace: ATS over NVLink-C2C), u and
+ *                   v are read and `out` is written by the kernels in place;
+ *                   only the texture is copied to the device.
  *   workspace       device scratch of at least rlic_workspace_bytes(...)
  *                   bytes, 256-byte aligned, or NULL to let the call allocate
  *                   it stream-ordered (cudaMallocAsync / cudaFreeAsync).

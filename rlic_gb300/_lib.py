@@ -67,6 +67,9 @@ class _Ops:
         return bool(np.any(~np.isfinite(a)))
 
 
+_NEGATIVE_TEXTURE = "Found invalid texture element(s). Expected only positive values."
+
+
 def _collect_problems(
     ops: _Ops,
     texture: Any,
@@ -76,8 +79,13 @@ def _collect_problems(
     uv_mode: Any,
     boundaries: Any,
     iterations: int,
+    check_negative: bool = True,
 ) -> tuple[list[Exception], BoundarySet | None]:
-    """All validation failures, in the reference's order (src/rlic/_lib.py:135-200)."""
+    """All validation failures, in the reference's order (src/rlic/_lib.py:135-200).
+
+    With check_negative=False the scan for negative texture elements is left
+    out (the caller then has it done on the GPU).
+    """
     problems: list[Exception] = []
     if iterations < 0:
         problems.append(
@@ -109,10 +117,8 @@ def _collect_problems(
         problems.append(
             ValueError(f"Expected a texture with exactly two dimensions. Got texture.ndim={texture.ndim!r}")
         )
-    if ops.any_negative(texture):
-        problems.append(
-            ValueError("Found invalid texture element(s). Expected only positive values.")
-        )
+    if check_negative and ops.any_negative(texture):
+        problems.append(ValueError(_NEGATIVE_TEXTURE))
     tshape, ushape, vshape = ops.shape(texture), ops.shape(u), ops.shape(v)
     if ushape != tshape or vshape != tshape:
         problems.append(
@@ -160,8 +166,16 @@ def _convolve_numpy(
     fn = lib.rlic_convolve_f32 if dtype == np.dtype("float32") else lib.rlic_convolve_f64
     rc = fn(
         _ptr(tex_c), _ptr(u_c), _ptr(v_c), ny, nx, _ptr(k_c), k_c.shape[0], uv_code,
-        *bcodes, iterations, _ptr(out), None, 0, None, _native.RLIC_FLAG_HOST_MEMORY,
+        *bcodes, iterations, _ptr(out), None, 0, None,
+        _native.RLIC_FLAG_HOST_MEMORY | _native.RLIC_FLAG_CHECK_TEXTURE,
     )
+    if rc == _native.RLIC_ERR_NEGATIVE_TEXTURE or (
+        rc != _native.RLIC_OK and np.any(texture < 0)
+    ):
+        # the only problem left (every other check passed on the host); it
+        # takes precedence over a failure of the native call, as validation
+        # does in the reference
+        raise ValueError(_NEGATIVE_TEXTURE)
     _native.check(rc)
     return out
 
@@ -246,9 +260,19 @@ def convolve(
     """
     use_torch = _is_torch(texture)
     ops = _Ops(use_torch)
+    # numpy inputs: the scan for negative texture elements runs on the GPU
+    # with the convolution (one pass over the uploaded texture instead of a
+    # host pass); it runs here only when the call fails anyway or never
+    # reaches the GPU, so the raised errors are always those of the reference
+    deferred = not use_torch and iterations != 0
     problems, bs = _collect_problems(
-        ops, texture, u, v, kernel, uv_mode, boundaries, iterations
+        ops, texture, u, v, kernel, uv_mode, boundaries, iterations,
+        check_negative=not deferred,
     )
+    if deferred and problems:
+        problems, bs = _collect_problems(
+            ops, texture, u, v, kernel, uv_mode, boundaries, iterations
+        )
     if len(problems) == 1:
         raise problems[0]
     if problems:

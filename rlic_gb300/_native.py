@@ -19,6 +19,7 @@ RLIC_ERR_INVALID_ARGUMENT = 1
 RLIC_ERR_CUDA = 2
 RLIC_ERR_OUT_OF_MEMORY = 3
 RLIC_ERR_WORKSPACE_TOO_SMALL = 4
+RLIC_ERR_NEGATIVE_TEXTURE = 5
 
 RLIC_UV_VELOCITY = 0
 RLIC_UV_POLARIZATION = 1
@@ -27,6 +28,7 @@ RLIC_FLAG_HOST_MEMORY = 0x1
 RLIC_FLAG_NO_FMA = 0x2
 RLIC_FLAG_NO_BRANCHLESS = 0x4
 RLIC_FLAG_NO_PATH_CACHE = 0x8
+RLIC_FLAG_CHECK_TEXTURE = 0x20
 
 RLIC_STORAGE_FP16 = 0
 RLIC_STORAGE_BF16 = 1

@@ -27,8 +27,11 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace rlic {
@@ -57,7 +60,8 @@ constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 constexpr unsigned kKnownFlags = RLIC_FLAG_HOST_MEMORY | RLIC_FLAG_NO_FMA |
-                                 RLIC_FLAG_NO_BRANCHLESS | RLIC_FLAG_NO_PATH_CACHE;
+                                 RLIC_FLAG_NO_BRANCHLESS | RLIC_FLAG_NO_PATH_CACHE |
+                                 RLIC_FLAG_CHECK_TEXTURE;
 
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -74,6 +78,50 @@ int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t e_ = (expr);                             \
         if (e_ != cudaSuccess) return cuda_fail(e_, #expr);  \
     } while (0)
+
+// Whether kernels may read and write the caller's pageable host memory
+// directly (per device, cached).  RLIC_NO_HOST_DIRECT=1 in the environment
+// turns it off.
+bool host_direct_access() {
+    static std::mutex mu;
+    static int cache[64];
+    static bool init = false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!init) {
+        for (int& c : cache) c = -1;
+        init = true;
+    }
+    if (cache[dev] < 0) {
+        int pageable = 0, tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+        cudaDeviceGetAttribute(&tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+        const char* off = std::getenv("RLIC_NO_HOST_DIRECT");
+        cache[dev] = (pageable && tables && !(off && off[0] == '1')) ? 1 : 0;
+    }
+    return cache[dev] == 1;
+}
+
+// Writes one byte per 4 KiB of [p, p + bytes) from a few host threads, so
+// that every page is mapped before the GPU (or a copy) writes the result.
+void touch_pages(void* p, size_t bytes) {
+    constexpr size_t kPage = 4096;
+    const size_t pages = (bytes + kPage - 1) / kPage;
+    unsigned hw = std::thread::hardware_concurrency();
+    const size_t nthreads = std::max<size_t>(1, std::min<size_t>({size_t(hw ? hw : 1), 8, pages / 256 + 1}));
+    auto work = [p, bytes, pages, nthreads](size_t t) {
+        volatile unsigned char* b = static_cast<unsigned char*>(p);
+        for (size_t k = t; k < pages; k += nthreads) {
+            const size_t off = k * kPage;
+            if (off < bytes) b[off] = 0;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto& th : pool) th.join();
+}
 
 Variant make_variant(unsigned flags, int uv_mode) {
     return Variant{!(flags & RLIC_FLAG_NO_FMA), !(flags & RLIC_FLAG_NO_BRANCHLESS),
@@ -142,12 +190,20 @@ WorkspaceLayout workspace_layout(int64_t ny, int64_t nx, int64_t klen, int64_t i
     return w;
 }
 
+struct NoHook {
+    void operator()() const {}
+};
+
 // Runs `iterations` passes on device memory.  `ws` holds the workspace.
-template <typename T>
+// The passes alternate between `out` and the workspace's ping-pong buffer;
+// when `final_out` is given, the last pass writes it instead (and `out` is
+// device scratch).  `before_last()` runs on the host just before the last
+// pass is launched.
+template <typename T, typename Hook = NoHook>
 int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
                const T* kernel, int64_t klen, const Variant& var, const int bnd[4],
                int64_t iterations, T* out, unsigned char* ws, unsigned flags,
-               cudaStream_t stream) {
+               cudaStream_t stream, Hook before_last = Hook{}, T* final_out = nullptr) {
     const int64_t n = ny * nx;
     if (iterations == 0) {
         RLIC_CUDA_TRY(cudaMemsetAsync(out, 0, size_t(n) * sizeof(T), stream));
@@ -164,6 +220,10 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     const T* src = texture;
     for (int64_t it = 0; it < iterations; ++it) {
         T* dst = ((iterations - 1 - it) % 2 == 0) ? out : tmp;
+        if (it + 1 == iterations) {
+            before_last();
+            if (final_out) dst = final_out;
+        }
         if (it == 0 || !cache) {
             RLIC_CUDA_TRY(rlic::launch_pass(var, cache ? rlic::kPassSampleRecord : rlic::kPassSample,
                                             src, uv, kernel, int(klen), sh, lc, dst, codes,
@@ -216,36 +276,72 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         return rc;
     }
 
-    // Host memory: one stream-ordered device block holds the inputs, the
-    // output and the workspace; the call returns once `out` holds the result.
+    // Host memory.  With pageable-memory access (Grace: ATS over NVLink-C2C,
+    // cudaDevAttrPageableMemoryAccess) the pack kernel reads u and v straight
+    // from the caller's memory and the last pass stores straight into `out`;
+    // only the texture, which every pass gathers from, is copied to HBM.
+    // Otherwise u, v and the result go through device copies.  Either way the
+    // host touches every page of `out` while the GPU runs the earlier passes,
+    // so that the result lands in mapped pages.  The call returns once `out`
+    // holds the result.
+    if (iterations == 0) {  // zeros, as the native core (src/lib.rs:425, 433)
+        if (flags & RLIC_FLAG_CHECK_TEXTURE)
+            for (size_t k = 0; k < n; ++k)
+                if (texture[k] < T(0))
+                    return fail(RLIC_ERR_NEGATIVE_TEXTURE,
+                                "Found invalid texture element(s). Expected only positive values.");
+        std::memset(out, 0, n * sizeof(T));
+        return RLIC_OK;
+    }
+    const bool direct = host_direct_access();
     const size_t a_img = align_up(n * sizeof(T));
-    const size_t total = 4 * a_img + wl.total;
+    const size_t total = (direct ? 2 : 4) * a_img + wl.total + kAlign;
     unsigned char* d = nullptr;
     RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d), total, stream));
     T* d_tex = reinterpret_cast<T*>(d);
-    T* d_u = reinterpret_cast<T*>(d + a_img);
-    T* d_v = reinterpret_cast<T*>(d + 2 * a_img);
-    T* d_out = reinterpret_cast<T*>(d + 3 * a_img);
-    unsigned char* ws = d + 4 * a_img;
+    T* d_out = reinterpret_cast<T*>(d + a_img);  // device ping-pong / result buffer
+    T* d_u = direct ? const_cast<T*>(u) : reinterpret_cast<T*>(d + 2 * a_img);
+    T* d_v = direct ? const_cast<T*>(v) : reinterpret_cast<T*>(d + 3 * a_img);
+    unsigned char* ws = d + (direct ? 2 : 4) * a_img;
     T* d_kernel = reinterpret_cast<T*>(ws + wl.kernel);
+    unsigned* d_flag = reinterpret_cast<unsigned*>(ws + wl.total);
+    bool prefaulted = false;
+    auto prefault = [&]() {
+        if (!prefaulted) touch_pages(out, n * sizeof(T));
+        prefaulted = true;
+    };
     auto body = [&]() -> int {
         RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex, texture, n * sizeof(T), cudaMemcpyHostToDevice, stream));
-        RLIC_CUDA_TRY(cudaMemcpyAsync(d_u, u, n * sizeof(T), cudaMemcpyHostToDevice, stream));
-        RLIC_CUDA_TRY(cudaMemcpyAsync(d_v, v, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+        if (!direct) {
+            RLIC_CUDA_TRY(cudaMemcpyAsync(d_u, u, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+            RLIC_CUDA_TRY(cudaMemcpyAsync(d_v, v, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+        }
         RLIC_CUDA_TRY(cudaMemcpyAsync(d_kernel, kernel, size_t(klen) * sizeof(T),
                                       cudaMemcpyHostToDevice, stream));
+        if (flags & RLIC_FLAG_CHECK_TEXTURE)
+            RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
         int r = run_device<T>(d_tex, d_u, d_v, ny, nx, d_kernel, klen, var, bnd, iterations,
-                              d_out, ws, flags, stream);
+                              d_out, ws, flags, stream, prefault, direct ? out : nullptr);
         if (r) return r;
-        RLIC_CUDA_TRY(cudaMemcpyAsync(out, d_out, n * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        prefault();
+        if (!direct)
+            RLIC_CUDA_TRY(cudaMemcpyAsync(out, d_out, n * sizeof(T), cudaMemcpyDeviceToHost, stream));
         return RLIC_OK;
     };
     rc = body();
+    unsigned negative = 0;
+    cudaError_t ec = cudaSuccess;
+    if (rc == RLIC_OK && (flags & RLIC_FLAG_CHECK_TEXTURE))
+        ec = cudaMemcpyAsync(&negative, d_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
     cudaError_t ef = cudaFreeAsync(d, stream);
     cudaError_t es = cudaStreamSynchronize(stream);
     if (rc) return rc;
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaMemcpyAsync");
     if (ef != cudaSuccess) return cuda_fail(ef, "cudaFreeAsync");
     if (es != cudaSuccess) return cuda_fail(es, "cudaStreamSynchronize");
+    if (negative)
+        return fail(RLIC_ERR_NEGATIVE_TEXTURE,
+                    "Found invalid texture element(s). Expected only positive values.");
     return RLIC_OK;
 }
 

@@ -351,6 +351,20 @@ lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
     for (int k = threadIdx.x; k < klen; k += blockDim.x) atomicAdd(dw + k, double(acc[k]));
 }
 
+// --------------------------------------------------------- input checks --
+
+// Sets *flag when some element of x is below zero (NaN is not: the same test
+// as numpy's `np.any(texture < 0)`, src/rlic/_lib.py:174).
+template <typename T>
+__global__ void check_negative_kernel(const T* __restrict__ x, int64_t n,
+                                      unsigned* __restrict__ flag) {
+    bool neg = false;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride)
+        neg |= x[k] < T(0);
+    if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
 // ------------------------------------------------ reduced-precision helpers --
 
 // Float copy of the kernel, 1/sum(|kernel|) as used by the reduced-precision
@@ -602,6 +616,16 @@ inline unsigned stream_blocks(int64_t n) {
 }
 
 template <typename T>
+cudaError_t launch_check_negative_t(const T* x, int64_t n, unsigned* flag, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    // whole warps only: every lane of a launched warp reaches the vote
+    check_negative_kernel<T><<<stream_blocks(n), 256, 0, stream>>>(x, n, flag);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_lowp_prepare_t(const T* kernel, int klen, int64_t iterations, float* w32,
                                   float* inv_scale, double* undo, cudaStream_t stream) {
     lowp_prepare_kernel<T><<<1, 256, 0, stream>>>(kernel, klen, iterations, w32, inv_scale, undo);
@@ -713,6 +737,10 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
     cudaError_t launch_from_storage(const void* src, int storage, const double* undo, T* dst, \
                                     int64_t n, cudaStream_t stream) {                        \
         return launch_from_storage_t<T>(src, storage, undo, dst, n, stream);                 \
+    }                                                                                        \
+    cudaError_t launch_check_negative(const T* x, int64_t n, unsigned* flag,                 \
+                                      cudaStream_t stream) {                                 \
+        return launch_check_negative_t<T>(x, n, flag, stream);                               \
     }                                                                                        \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel, int klen, \
                                const Shape& sh, T* y, cudaStream_t stream) {                 \

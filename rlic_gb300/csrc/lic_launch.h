@@ -71,6 +71,8 @@ inline int64_t code_words_per_pixel(int64_t klen) {
                                   cudaStream_t stream);                                    \
     cudaError_t launch_from_storage(const void* src, int storage, const double* undo,      \
                                     T* dst, int64_t n, cudaStream_t stream);               \
+    cudaError_t launch_check_negative(const T* x, int64_t n, unsigned* flag,               \
+                                      cudaStream_t stream);                                \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel,         \
                                int klen, const Shape& sh, T* y, cudaStream_t stream);      \
     cudaError_t launch_kernel_grad(const T* g, const T* x, const uint32_t* codes,          \

@@ -321,7 +321,8 @@ def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
     rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
-    assert _native.launch_count() - before == 4  # pack + traced pass + 2 replays
+    # texture check + pack + traced pass + 2 replays
+    assert _native.launch_count() - before == 5
 
 
 def test_device_entry_points_with_workspace(oracle) -> None:
@@ -371,3 +372,49 @@ def test_device_entry_points_with_workspace(oracle) -> None:
     want2 = oracle.convolve(tex2.cpu().numpy(), u, v, k, uv_mode="polarization",
                             boundaries="periodic")
     assert_bitwise(out.cpu().numpy(), want2)
+
+
+def test_host_path_checks_negative_texture_on_device() -> None:
+    rng = np.random.default_rng(31)
+    tex = rng.random((64, 80))
+    u, v = _field(rng, 64, 80, np.float64, "random")
+    k = np.hanning(9)
+    bad = tex.copy()
+    bad[17, 3] = -1e-300
+    with pytest.raises(ValueError, match=r"^Found invalid texture element\(s\)\. Expected only positive values\.$"):
+        rlic_gb300.convolve(bad, u, v, kernel=k, iterations=2)
+    # -0.0 and NaN are not below zero: no error, as np.any(texture < 0)
+    ok = tex.copy()
+    ok[0, 0] = -0.0
+    ok[1, 1] = np.nan
+    out = rlic_gb300.convolve(ok, u, v, kernel=k)
+    assert out.shape == ok.shape
+    # several problems at once are still grouped on the host, in order
+    with pytest.raises(ExceptionGroup) as info:
+        rlic_gb300.convolve(bad, u, v, kernel=k, iterations=-1)
+    assert [type(e) for e in info.value.exceptions] == [ValueError, ValueError]
+
+
+def test_host_path_without_direct_access(tmp_path) -> None:
+    """The copy-based host path (devices without pageable-memory access) gives
+    the same bits as the direct one."""
+    import subprocess
+    import sys
+
+    script = tmp_path / "noh.py"
+    script.write_text(
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {str(Path(__file__).resolve().parents[1])!r})\n"
+        "import rlic_gb300\n"
+        "from rlic_gb300.workloads import readme_case\n"
+        "c = readme_case(n=96)\n"
+        "out = rlic_gb300.convolve(c['texture'], c['u'], c['v'], kernel=c['kernel'],\n"
+        "                          boundaries='periodic', iterations=3)\n"
+        f"np.save({str(tmp_path / 'out.npy')!r}, out)\n"
+    )
+    env = dict(__import__("os").environ, RLIC_NO_HOST_DIRECT="1")
+    subprocess.run([sys.executable, str(script)], check=True, env=env, timeout=300)
+    c = readme_case(n=96)
+    want = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                               boundaries="periodic", iterations=3)
+    assert_bitwise(np.load(tmp_path / "out.npy"), want)
