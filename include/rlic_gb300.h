@@ -54,6 +54,7 @@ extern "C" {
 #define RLIC_ERR_OUT_OF_MEMORY 3
 #define RLIC_ERR_WORKSPACE_TOO_SMALL 4
 #define RLIC_ERR_NEGATIVE_TEXTURE 5
+#define RLIC_ERR_UNSUPPORTED 6
 
 /* uv_mode: src/lib.rs:14-27 ("velocity" / "polarization") */
 #define RLIC_UV_VELOCITY 0
@@ -274,6 +275,35 @@ RLIC_API int rlic_convolve_f32_noalloc(const float *texture, const float *u, con
                                        int64_t klen, int uv_mode, int bx_left, int bx_right,
                                        int by_left, int by_right, int64_t iterations,
                                        float *out, void *stream, unsigned flags);
+
+/*
+ * rlic_convolve_* on strided host arrays, read in place (no host copies):
+ * numpy views such as broadcasts (stride 0, as in the reference's README
+ * example), transposes, reversed or sliced arrays.  strides[6] holds the
+ * element strides (row, column) of texture, u and v, in that order; `out` is
+ * C-contiguous.  Requires RLIC_FLAG_HOST_MEMORY and a device that can access
+ * pageable host memory (rlic_host_direct_access() == 1; otherwise
+ * RLIC_ERR_UNSUPPORTED).  Other arguments and flags as rlic_convolve_*; the
+ * call allocates its scratch and returns once `out` holds the result.
+ */
+RLIC_API int rlic_convolve_strided_f32(const float *texture, const float *u, const float *v,
+                                       const int64_t *strides, int64_t ny, int64_t nx,
+                                       const float *kernel, int64_t klen, int uv_mode,
+                                       int bx_left, int bx_right, int by_left, int by_right,
+                                       int64_t iterations, float *out, void *stream,
+                                       unsigned flags);
+RLIC_API int rlic_convolve_strided_f64(const double *texture, const double *u,
+                                       const double *v, const int64_t *strides, int64_t ny,
+                                       int64_t nx, const double *kernel, int64_t klen,
+                                       int uv_mode, int bx_left, int bx_right, int by_left,
+                                       int by_right, int64_t iterations, double *out,
+                                       void *stream, unsigned flags);
+
+/* 1 when kernels on the current device can read and write pageable host
+ * memory directly (Grace: ATS over NVLink-C2C) and RLIC_NO_HOST_DIRECT is not
+ * set to 1; then host-memory calls read u, v (and strided inputs) in place
+ * and write the result in place. */
+RLIC_API int rlic_host_direct_access(void);
 
 /*
  * Streamline cells, for index-for-index parity checks of the trace

@@ -146,6 +146,14 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
+def _element_strides(a: np.ndarray) -> tuple[int, int] | None:
+    """(row, column) strides in elements, or None when not whole elements."""
+    its = a.itemsize
+    if any(st % its for st in a.strides):
+        return None
+    return a.strides[0] // its, a.strides[1] // its
+
+
 def _convolve_numpy(
     texture: np.ndarray,
     u: np.ndarray,
@@ -157,18 +165,31 @@ def _convolve_numpy(
 ) -> np.ndarray:
     lib = _native.lib()
     dtype = texture.dtype
-    tex_c = np.ascontiguousarray(texture)
-    u_c = np.ascontiguousarray(u)
-    v_c = np.ascontiguousarray(v)
     k_c = np.ascontiguousarray(kernel)
-    out = np.empty(tex_c.shape, dtype=dtype)
-    ny, nx = tex_c.shape
-    fn = lib.rlic_convolve_f32 if dtype == np.dtype("float32") else lib.rlic_convolve_f64
-    rc = fn(
-        _ptr(tex_c), _ptr(u_c), _ptr(v_c), ny, nx, _ptr(k_c), k_c.shape[0], uv_code,
-        *bcodes, iterations, _ptr(out), None, 0, None,
-        _native.RLIC_FLAG_HOST_MEMORY | _native.RLIC_FLAG_CHECK_TEXTURE,
-    )
+    ny, nx = texture.shape
+    out = np.empty((ny, nx), dtype=dtype)
+    flags = _native.RLIC_FLAG_HOST_MEMORY | _native.RLIC_FLAG_CHECK_TEXTURE
+    f32 = dtype == np.dtype("float32")
+    views = (texture, u, v)
+    strides = [_element_strides(a) for a in views]
+    contiguous = all(a.flags.c_contiguous for a in views)
+    if not contiguous and all(s is not None for s in strides) and lib.rlic_host_direct_access():
+        # strided views (broadcasts, transposes, slices) are read in place
+        st = (ctypes.c_int64 * 6)(*(x for s in strides for x in s))
+        fn = lib.rlic_convolve_strided_f32 if f32 else lib.rlic_convolve_strided_f64
+        rc = fn(
+            _ptr(texture), _ptr(u), _ptr(v), st, ny, nx, _ptr(k_c), k_c.shape[0], uv_code,
+            *bcodes, iterations, _ptr(out), None, flags,
+        )
+    else:
+        tex_c = np.ascontiguousarray(texture)
+        u_c = np.ascontiguousarray(u)
+        v_c = np.ascontiguousarray(v)
+        fn = lib.rlic_convolve_f32 if f32 else lib.rlic_convolve_f64
+        rc = fn(
+            _ptr(tex_c), _ptr(u_c), _ptr(v_c), ny, nx, _ptr(k_c), k_c.shape[0], uv_code,
+            *bcodes, iterations, _ptr(out), None, 0, None, flags,
+        )
     if rc == _native.RLIC_ERR_NEGATIVE_TEXTURE or (
         rc != _native.RLIC_OK and np.any(texture < 0)
     ):

@@ -20,6 +20,7 @@ RLIC_ERR_CUDA = 2
 RLIC_ERR_OUT_OF_MEMORY = 3
 RLIC_ERR_WORKSPACE_TOO_SMALL = 4
 RLIC_ERR_NEGATIVE_TEXTURE = 5
+RLIC_ERR_UNSUPPORTED = 6
 
 RLIC_UV_VELOCITY = 0
 RLIC_UV_POLARIZATION = 1
@@ -57,6 +58,11 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_path_code_bytes": ([_I64, _I64, _I64], _SZ),
     "rlic_convolve_f32": (_CONVOLVE_ARGS, _INT),
     "rlic_convolve_f64": (_CONVOLVE_ARGS, _INT),
+    "rlic_convolve_strided_f32": ([_P, _P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
+                                   _INT, _I64, _P, _P, _U], _INT),
+    "rlic_convolve_strided_f64": ([_P, _P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
+                                   _INT, _I64, _P, _P, _U], _INT),
+    "rlic_host_direct_access": ([], _INT),
     "rlic_trace_cells_f32": (_TRACE_ARGS, _INT),
     "rlic_trace_cells_f64": (_TRACE_ARGS, _INT),
     "rlic_pack_field_f32": ([_P, _P, _I64, _I64, _P, _P], _INT),

@@ -203,7 +203,8 @@ template <typename T, typename Hook = NoHook>
 int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
                const T* kernel, int64_t klen, const Variant& var, const int bnd[4],
                int64_t iterations, T* out, unsigned char* ws, unsigned flags,
-               cudaStream_t stream, Hook before_last = Hook{}, T* final_out = nullptr) {
+               cudaStream_t stream, Hook before_last = Hook{}, T* final_out = nullptr,
+               bool uv_ready = false) {
     const int64_t n = ny * nx;
     if (iterations == 0) {
         RLIC_CUDA_TRY(cudaMemsetAsync(out, 0, size_t(n) * sizeof(T), stream));
@@ -216,7 +217,7 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     const bool cache = use_path_cache(iterations, klen, flags);
     const Shape sh = make_shape(ny, nx, bnd);
     const LaunchConfig lc = launch_config();
-    RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream));
+    if (!uv_ready) RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream));
     const T* src = texture;
     for (int64_t it = 0; it < iterations; ++it) {
         T* dst = ((iterations - 1 - it) % 2 == 0) ? out : tmp;
@@ -237,11 +238,13 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     return RLIC_OK;
 }
 
+// `strides` (host memory only): element strides (row, column) of texture,
+// u and v, or NULL for C-contiguous arrays.
 template <typename T>
 int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
                   const T* kernel, int64_t klen, int uv_mode, int bxl, int bxr, int byl,
                   int byr, int64_t iterations, T* out, void* workspace, size_t workspace_bytes_,
-                  void* stream_, unsigned flags) {
+                  void* stream_, unsigned flags, const int64_t* strides = nullptr) {
     g_last_error.clear();
     const int bnd[4] = {bxl, bxr, byl, byr};
     int rc = check_common(ny, nx, klen, uv_mode, bnd, flags);
@@ -284,16 +287,23 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
     // host touches every page of `out` while the GPU runs the earlier passes,
     // so that the result lands in mapped pages.  The call returns once `out`
     // holds the result.
+    const int64_t contiguous[6] = {nx, 1, nx, 1, nx, 1};
+    const int64_t* st = strides ? strides : contiguous;
+    const bool strided = std::memcmp(st, contiguous, sizeof(contiguous)) != 0;
     if (iterations == 0) {  // zeros, as the native core (src/lib.rs:425, 433)
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
-            for (size_t k = 0; k < n; ++k)
-                if (texture[k] < T(0))
-                    return fail(RLIC_ERR_NEGATIVE_TEXTURE,
-                                "Found invalid texture element(s). Expected only positive values.");
+            for (int64_t i = 0; i < ny; ++i)
+                for (int64_t j = 0; j < nx; ++j)
+                    if (texture[i * st[0] + j * st[1]] < T(0))
+                        return fail(RLIC_ERR_NEGATIVE_TEXTURE,
+                                    "Found invalid texture element(s). Expected only positive values.");
         std::memset(out, 0, n * sizeof(T));
         return RLIC_OK;
     }
     const bool direct = host_direct_access();
+    if (strided && !direct)
+        return fail(RLIC_ERR_UNSUPPORTED,
+                    "strided host arrays need a device with pageable-memory access");
     const size_t a_img = align_up(n * sizeof(T));
     const size_t total = (direct ? 2 : 4) * a_img + wl.total + kAlign;
     unsigned char* d = nullptr;
@@ -311,7 +321,14 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         prefaulted = true;
     };
     auto body = [&]() -> int {
-        RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex, texture, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+        if (strided) {
+            RLIC_CUDA_TRY(rlic::launch_gather_strided(texture, st[0], st[1], d_tex, ny, nx, stream));
+            RLIC_CUDA_TRY(rlic::launch_pack_strided(u, st[2], st[3], v, st[4], st[5],
+                                                    ws + wl.uv, ny, nx, stream));
+        } else {
+            RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex, texture, n * sizeof(T), cudaMemcpyHostToDevice,
+                                          stream));
+        }
         if (!direct) {
             RLIC_CUDA_TRY(cudaMemcpyAsync(d_u, u, n * sizeof(T), cudaMemcpyHostToDevice, stream));
             RLIC_CUDA_TRY(cudaMemcpyAsync(d_v, v, n * sizeof(T), cudaMemcpyHostToDevice, stream));
@@ -321,7 +338,8 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
             RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
         int r = run_device<T>(d_tex, d_u, d_v, ny, nx, d_kernel, klen, var, bnd, iterations,
-                              d_out, ws, flags, stream, prefault, direct ? out : nullptr);
+                              d_out, ws, flags, stream, prefault, direct ? out : nullptr,
+                              strided);
         if (r) return r;
         prefault();
         if (!direct)
@@ -839,6 +857,34 @@ int rlic_convolve_f64(const double* texture, const double* u, const double* v, i
                                  bx_right, by_left, by_right, iterations, out, workspace,
                                  workspace_bytes, stream, flags);
 }
+
+int rlic_convolve_strided_f32(const float* texture, const float* u, const float* v,
+                              const int64_t* strides, int64_t ny, int64_t nx,
+                              const float* kernel, int64_t klen, int uv_mode, int bx_left,
+                              int bx_right, int by_left, int by_right, int64_t iterations,
+                              float* out, void* stream, unsigned flags) {
+    if (!strides) return fail(RLIC_ERR_INVALID_ARGUMENT, "null strides");
+    if (!(flags & RLIC_FLAG_HOST_MEMORY))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "strided arrays are host memory only");
+    return convolve_impl<float>(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left, bx_right,
+                                by_left, by_right, iterations, out, nullptr, 0, stream, flags,
+                                strides);
+}
+
+int rlic_convolve_strided_f64(const double* texture, const double* u, const double* v,
+                              const int64_t* strides, int64_t ny, int64_t nx,
+                              const double* kernel, int64_t klen, int uv_mode, int bx_left,
+                              int bx_right, int by_left, int by_right, int64_t iterations,
+                              double* out, void* stream, unsigned flags) {
+    if (!strides) return fail(RLIC_ERR_INVALID_ARGUMENT, "null strides");
+    if (!(flags & RLIC_FLAG_HOST_MEMORY))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "strided arrays are host memory only");
+    return convolve_impl<double>(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left,
+                                 bx_right, by_left, by_right, iterations, out, nullptr, 0,
+                                 stream, flags, strides);
+}
+
+int rlic_host_direct_access(void) { return host_direct_access() ? 1 : 0; }
 
 int rlic_trace_cells_f32(const float* u, const float* v, int64_t ny, int64_t nx, int64_t klen,
                          int uv_mode, int bx_left, int bx_right, int by_left, int by_right,

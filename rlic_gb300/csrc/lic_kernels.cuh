@@ -351,6 +351,47 @@ lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
     for (int k = threadIdx.x; k < klen; k += blockDim.x) atomicAdd(dw + k, double(acc[k]));
 }
 
+// ------------------------------------------------------- strided inputs --
+//
+// Inputs given as strided views (element strides, possibly zero or
+// negative: numpy broadcasts, transposes, reversed or sliced arrays) are read
+// in place, from device memory or, on devices with pageable-memory access,
+// from the caller's host memory.  A zero stride re-reads the same elements,
+// which then come from cache.
+
+template <typename T>
+__global__ void pack_uv_strided_kernel(const T* __restrict__ u, int64_t su0, int64_t su1,
+                                       const T* __restrict__ v, int64_t sv0, int64_t sv1,
+                                       typename Vec2<T>::type* __restrict__ uv, int64_t ny,
+                                       int64_t nx) {
+    for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
+        for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nx;
+             j += int64_t(gridDim.x) * blockDim.x) {
+            typename Vec2<T>::type p;
+            p.x = u[i * su0 + j * su1];
+            p.y = v[i * sv0 + j * sv1];
+            uv[i * nx + j] = p;
+        }
+    }
+}
+
+template <typename T>
+__global__ void gather_strided_kernel(const T* __restrict__ src, int64_t s0, int64_t s1,
+                                      T* __restrict__ dst, int64_t ny, int64_t nx) {
+    for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
+        for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nx;
+             j += int64_t(gridDim.x) * blockDim.x)
+            dst[i * nx + j] = src[i * s0 + j * s1];
+    }
+}
+
+inline dim3 rows_grid(int64_t ny, int64_t nx) {
+    int64_t gx = (nx + 255) / 256;
+    if (gx > 64) gx = 64;
+    int64_t gy = ny < 65535 ? ny : 65535;
+    return dim3(unsigned(gx < 1 ? 1 : gx), unsigned(gy < 1 ? 1 : gy));
+}
+
 // --------------------------------------------------------- input checks --
 
 // Sets *flag when some element of x is below zero (NaN is not: the same test
@@ -616,6 +657,24 @@ inline unsigned stream_blocks(int64_t n) {
 }
 
 template <typename T>
+cudaError_t launch_pack_strided_t(const T* u, int64_t su0, int64_t su1, const T* v, int64_t sv0,
+                                  int64_t sv1, void* uv, int64_t ny, int64_t nx,
+                                  cudaStream_t stream) {
+    pack_uv_strided_kernel<T><<<rows_grid(ny, nx), 256, 0, stream>>>(
+        u, su0, su1, v, sv0, sv1, static_cast<typename Vec2<T>::type*>(uv), ny, nx);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gather_strided_t(const T* src, int64_t s0, int64_t s1, T* dst, int64_t ny,
+                                    int64_t nx, cudaStream_t stream) {
+    gather_strided_kernel<T><<<rows_grid(ny, nx), 256, 0, stream>>>(src, s0, s1, dst, ny, nx);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_check_negative_t(const T* x, int64_t n, unsigned* flag, cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
@@ -741,6 +800,15 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
     cudaError_t launch_check_negative(const T* x, int64_t n, unsigned* flag,                 \
                                       cudaStream_t stream) {                                 \
         return launch_check_negative_t<T>(x, n, flag, stream);                               \
+    }                                                                                        \
+    cudaError_t launch_pack_strided(const T* u, int64_t su0, int64_t su1, const T* v,        \
+                                    int64_t sv0, int64_t sv1, void* uv, int64_t ny,          \
+                                    int64_t nx, cudaStream_t stream) {                       \
+        return launch_pack_strided_t<T>(u, su0, su1, v, sv0, sv1, uv, ny, nx, stream);       \
+    }                                                                                        \
+    cudaError_t launch_gather_strided(const T* src, int64_t s0, int64_t s1, T* dst,          \
+                                      int64_t ny, int64_t nx, cudaStream_t stream) {         \
+        return launch_gather_strided_t<T>(src, s0, s1, dst, ny, nx, stream);                 \
     }                                                                                        \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel, int klen, \
                                const Shape& sh, T* y, cudaStream_t stream) {                 \

@@ -320,9 +320,15 @@ def test_strided_and_broadcast_inputs(oracle) -> None:
 def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
-    rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
+    u, v = np.ascontiguousarray(c["u"]), np.ascontiguousarray(c["v"])
+    rlic_gb300.convolve(c["texture"], u, v, kernel=c["kernel"], iterations=3)
     # texture check + pack + traced pass + 2 replays
     assert _native.launch_count() - before == 5
+    before = _native.launch_count()
+    rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
+    # broadcast u, v: read in place (strided gather + strided pack) where the
+    # device reaches host memory, else copied (plain pack)
+    assert _native.launch_count() - before == (6 if _native.lib().rlic_host_direct_access() else 5)
 
 
 def test_device_entry_points_with_workspace(oracle) -> None:
@@ -418,3 +424,32 @@ def test_host_path_without_direct_access(tmp_path) -> None:
     want = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
                                boundaries="periodic", iterations=3)
     assert_bitwise(np.load(tmp_path / "out.npy"), want)
+
+
+def test_strided_views_read_in_place(oracle) -> None:
+    """Broadcast, transposed, reversed and sliced numpy views give the bits of
+    their contiguous copies (read in place where the device can reach host
+    memory, copied otherwise)."""
+    c = readme_case(n=300)
+    big = np.random.default_rng(41).random((600, 700))
+    views = {
+        "broadcast_uv": (c["texture"], c["u"], c["v"]),
+        "transposed": (big[:300, :300].T, c["u"].T, c["v"].T),
+        "reversed_sliced": (big[::-2, 5:605:2], np.ascontiguousarray(c["u"])[::-1, ::-1],
+                            np.ascontiguousarray(c["v"])[:, ::-1]),
+        "broadcast_texture": (np.broadcast_to(big[0, :300], (300, 300)), c["u"], c["v"]),
+    }
+    for name, (t, u, v) in views.items():
+        for dtype in (np.float64, np.float32):
+            t_, u_, v_ = (np.asarray(a, dtype=dtype) if a.dtype != dtype else a for a in (t, u, v))
+            k = c["kernel"].astype(dtype)
+            got = rlic_gb300.convolve(t_, u_, v_, kernel=k, uv_mode="polarization",
+                                      boundaries={"x": "periodic", "y": "closed"}, iterations=2)
+            want = rlic_gb300.convolve(np.ascontiguousarray(t_), np.ascontiguousarray(u_),
+                                       np.ascontiguousarray(v_), kernel=k, uv_mode="polarization",
+                                       boundaries={"x": "periodic", "y": "closed"}, iterations=2)
+            assert_bitwise(got, want)
+    # and the contiguous result is the oracle's
+    t, u, v = views["transposed"]
+    want = oracle.convolve(np.ascontiguousarray(t), u, v, c["kernel"], iterations=1)
+    assert_bitwise(rlic_gb300.convolve(t, u, v, kernel=c["kernel"]), want)
