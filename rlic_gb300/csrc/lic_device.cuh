@@ -39,6 +39,38 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
 __device__ __forceinline__ double abs_(double a) { return fabs(a); }
 
+// Packed pairs of float32 operations (sm_100-family f32x2 instructions): each
+// lane is rounded exactly as the scalar __fmaf_rn / __fsub_rn / __fmul_rn.
+// The x and y halves of a streamline step are independent, so they share one
+// instruction.
+__device__ __forceinline__ float2 fma2_rn(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{.reg .b64 pa, pb, pc, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\tmov.b64 pc, {%6, %7};\n\t"
+        "fma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) {
+    float2 r;
+    asm("{.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+    float2 r;
+    asm("{.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
 // Accumulation of one kernel-weighted sample: `mul_add` in the default build
 // (src/lib.rs:357-360, 380-383), a rounded product then a rounded sum without
 // the `fma` feature (src/lib.rs:353-356, 376-379).
@@ -121,6 +153,23 @@ __device__ __forceinline__ T time_to_next_pixel(T vel, T frac) {
     }
 }
 
+// Both times of one step, tx for (u, fx) and ty for (v, fy).  The default
+// float32 build computes the x and y halves of the branchless formula as
+// packed pairs; every other case is time_to_next_pixel twice.
+template <typename T, bool FMA, bool BRANCHLESS>
+__device__ __forceinline__ void times_to_next_pixel(T u, T v, T fx, T fy, T& tx, T& ty) {
+    if constexpr (BRANCHLESS && FMA && sizeof(T) == 4) {
+        const float2 s = make_float2(signbit(u) ? 0.f : 2.f, signbit(v) ? 0.f : 2.f);
+        const float2 f = make_float2(fx, fy);
+        const float2 rem = fma2_rn(s, sub2_rn(make_float2(0.5f, 0.5f), f), f);
+        tx = abs_quotient(rem.x, float(u));
+        ty = abs_quotient(rem.y, float(v));
+    } else {
+        tx = time_to_next_pixel<T, FMA, BRANCHLESS>(u, fx);
+        ty = time_to_next_pixel<T, FMA, BRANCHLESS>(v, fy);
+    }
+}
+
 // One image axis with its two boundary rules (BoundaryPair, src/lib.rs:70-96),
 // pre-resolved: a coordinate that stepped to -1 becomes `lo_to`, one that
 // stepped to `size` becomes `hi_to` (closed: clamp; periodic: wrap).  The
@@ -149,13 +198,15 @@ struct Geometry {
     Axis<I> ax, ay;
 };
 
-// Step codes of the path cache: 4 bits per streamline step.
-//   0      no move (zero velocity, or a move cancelled by a closed boundary)
-//   1, 2   +1 / -1 column            3, 4   +1 / -1 row
-//   5, 6   wrap right -> left (-(nx-1)) / left -> right (+(nx-1))
-//   7, 8   wrap bottom -> top (-(ny-1) rows) / top -> bottom (+(ny-1) rows)
-//   15     the trace stopped on a NaN sample (this and all later steps)
-// The linear-index delta of each code is in the table below; replaying the
+// Step codes of the path cache: 4 bits per streamline step, two 2-bit
+// fields: bits 0-1 the column move dx, bits 2-3 the row move dy, each 00 = 0,
+// 01 = +1, 11 = -1 (two's complement), 10 = a wrap across a periodic edge.
+//   0x0    no move (zero velocity, or a move cancelled by a closed boundary)
+//   0x1, 0x3   +1 / -1 column         0x4, 0xC   +1 / -1 row
+//   0x2, 0x6   wrap right -> left (-(nx-1)) / left -> right (+(nx-1))
+//   0x8, 0x9   wrap bottom -> top (-(ny-1) rows) / top -> bottom (+(ny-1) rows)
+//   0xF    the trace stopped on a NaN sample (a step never moves both axes)
+// The table below maps every code to its linear-index delta.  Replaying the
 // deltas from the start pixel visits exactly the cells the trace visited.
 constexpr uint32_t kStop = 15u;
 
@@ -163,14 +214,14 @@ template <typename I>
 __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
     // called by one thread
     for (int c = 0; c < 16; ++c) table[c] = 0;
-    table[1] = 1;
-    table[2] = -1;
-    table[3] = nx;
-    table[4] = -nx;
-    table[5] = -(nx - 1);
-    table[6] = nx - 1;
-    table[7] = -(ny - 1) * nx;
-    table[8] = (ny - 1) * nx;
+    table[0x1] = 1;
+    table[0x3] = -1;
+    table[0x4] = nx;
+    table[0xC] = -nx;
+    table[0x2] = -(nx - 1);
+    table[0x6] = nx - 1;
+    table[0x8] = -(ny - 1) * nx;
+    table[0x9] = (ny - 1) * nx;
 }
 
 // advance, src/lib.rs:236-273, with update_state (src/lib.rs:209-233) folded
@@ -197,29 +248,36 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     // takes the slow one) and its lane in step with the warp.
     const T su = still ? T(1) : u;
     const T sv = still ? T(1) : v;
-    const T tx = time_to_next_pixel<T, FMA, BRANCHLESS>(su, fx);
-    const T ty = time_to_next_pixel<T, FMA, BRANCHLESS>(sv, fy);
+    T tx, ty;
+    times_to_next_pixel<T, FMA, BRANCHLESS>(su, sv, fx, fy, tx, ty);
     const bool xstep = tx < ty;
-    const T vpar = xstep ? su : sv;
-    const T vorth = xstep ? sv : su;
     const T t = xstep ? tx : ty;
-    const T forth_in = xstep ? fy : fx;
-    T forth;
-    if constexpr (FMA) {
-        forth = fma_rn(t, vorth, forth_in);
+    // the orthogonal update of either branch (update_state, src/lib.rs:225-232):
+    // an x step moves fy by t * v, a y step moves fx by t * u; both are
+    // computed and the branch keeps one
+    T cx, cy;
+    if constexpr (FMA && sizeof(T) == 4) {
+        const float2 c = fma2_rn(make_float2(t, t), make_float2(su, sv), make_float2(fx, fy));
+        cx = c.x;
+        cy = c.y;
+    } else if constexpr (FMA) {
+        cx = fma_rn(t, su, fx);
+        cy = fma_rn(t, sv, fy);
     } else {
-        forth = add_rn(forth_in, mul_rn(t, vorth));
+        cx = add_rn(fx, mul_rn(t, su));
+        cy = add_rn(fy, mul_rn(t, sv));
     }
+    const T vpar = xstep ? su : sv;
     const bool up = vpar >= T(0);
     const T fpar = up ? T(0) : T(1);
-    const T nfx = xstep ? fpar : forth;
-    const T nfy = xstep ? forth : fpar;
+    const T nfx = xstep ? fpar : cx;
+    const T nfy = xstep ? cy : fpar;
     fx = still ? fx : nfx;
     fy = still ? fy : nfy;
     if constexpr (!EDGE) {
         const I step = xstep ? I(1) : g.nx;
         cell += still ? I(0) : (up ? step : -step);
-        const uint32_t code = xstep ? (up ? 1u : 2u) : (up ? 3u : 4u);
+        const uint32_t code = xstep ? (up ? 0x1u : 0x3u) : (up ? 0x4u : 0xCu);
         return still ? 0u : code;
     } else {
         const I c_old = xstep ? j : i;
@@ -241,13 +299,13 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
         if (dd == I(0)) {
             code = 0u;
         } else if (dd == I(1)) {
-            code = xstep ? 1u : 3u;
+            code = xstep ? 0x1u : 0x4u;
         } else if (dd == I(-1)) {
-            code = xstep ? 2u : 4u;
+            code = xstep ? 0x3u : 0xCu;
         } else if (dd < I(0)) {
-            code = xstep ? 5u : 7u;
+            code = xstep ? 0x2u : 0x8u;
         } else {
-            code = xstep ? 6u : 8u;
+            code = xstep ? 0x6u : 0x9u;
         }
         return code;
     }
@@ -277,7 +335,13 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
     T pu = p.x, pv = p.y;
     if (isnan(pu) || isnan(pv)) return false;
     if constexpr (POL) {
-        const T dot = add_rn(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
+        T dot;
+        if constexpr (sizeof(T) == 4) {
+            const float2 pr = mul2_rn(make_float2(pu, pv), make_float2(st.lu, st.lv));
+            dot = add_rn(pr.x, pr.y);
+        } else {
+            dot = add_rn(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
+        }
         if (dot < T(0)) {
             pu = -pu;
             pv = -pv;

@@ -41,7 +41,20 @@
 
 namespace rlic {
 
+// Minimum resident CTAs per SM for the float32 / 32-bit-index replay
+// kernel's register allocation (8: 32 registers, full occupancy; measured
+// fastest at 8192^2).  Wider types need more registers and keep fewer CTAs.
+#ifndef RLIC_GATHER_MIN_BLOCKS
+#define RLIC_GATHER_MIN_BLOCKS 8
+#endif
+
 template <typename T> struct PassMinBlocks { static constexpr int value = 1; };
+
+template <typename T, typename I> struct GatherMinBlocks { static constexpr int value = 4; };
+template <> struct GatherMinBlocks<float, int32_t> {
+    static constexpr int value = RLIC_GATHER_MIN_BLOCKS;
+};
+template <> struct GatherMinBlocks<float, int64_t> { static constexpr int value = 6; };
 template <> struct PassMinBlocks<float> { static constexpr int value = RLIC_PASS_MIN_BLOCKS_F32; };
 
 template <typename T>
@@ -221,7 +234,7 @@ __device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restr
 }
 
 template <typename T, bool FMA, typename I>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (GatherMinBlocks<T, I>::value))
 lic_gather_kernel(const T* __restrict__ tex_in, const uint32_t* __restrict__ codes,
                   const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
                   T* __restrict__ tex_out, CodeLayout cl) {
