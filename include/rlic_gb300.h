@@ -131,7 +131,8 @@ RLIC_API size_t rlic_path_code_bytes(int64_t ny, int64_t nx, int64_t klen);
  *                   only the texture is copied to the device.
  *   workspace       device scratch of at least rlic_workspace_bytes(...)
  *                   bytes, 256-byte aligned, or NULL to let the call allocate
- *                   it stream-ordered (cudaMallocAsync / cudaFreeAsync).
+ *                   it stream-ordered from the library's memory pool (see
+ *                   rlic_release_cached_memory).
  *                   Ignored with RLIC_FLAG_HOST_MEMORY (the call allocates).
  */
 RLIC_API int rlic_convolve_f32(const float *texture, const float *u, const float *v, int64_t ny,
@@ -375,6 +376,25 @@ RLIC_API int rlic_set_block_shape(int block_x, int block_y);
  * a caller confirm that work ran on the device and count launches per call.
  */
 RLIC_API uint64_t rlic_kernel_launch_count(void);
+
+/*
+ * Page-locked host buffers for results: rlic_host_buffer_alloc returns a
+ * pinned block of `bytes` (NULL on failure), reusing a block of the same size
+ * released earlier by rlic_host_buffer_free.  Host-memory calls that write
+ * into such a block need no page faults and no staging copy.  At most 4 GiB
+ * of released blocks are kept.
+ */
+RLIC_API void *rlic_host_buffer_alloc(size_t bytes);
+RLIC_API void rlic_host_buffer_free(void *p);
+
+/*
+ * Calls that allocate their scratch (a NULL workspace, host-memory calls)
+ * draw it from a stream-ordered memory pool owned by the library, one per
+ * device, which keeps freed memory for later calls.  This returns the
+ * current device's cached device memory to the driver (after a device-wide
+ * synchronisation) and frees the released host buffers.
+ */
+RLIC_API int rlic_release_cached_memory(void);
 
 #ifdef __cplusplus
 }

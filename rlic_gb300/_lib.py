@@ -167,7 +167,8 @@ def _convolve_numpy(
     dtype = texture.dtype
     k_c = np.ascontiguousarray(kernel)
     ny, nx = texture.shape
-    out = np.empty((ny, nx), dtype=dtype)
+    # a page-locked result buffer, reused once the caller drops an earlier one
+    out = _native.pinned_empty((ny, nx), dtype)
     flags = _native.RLIC_FLAG_HOST_MEMORY | _native.RLIC_FLAG_CHECK_TEXTURE
     f32 = dtype == np.dtype("float32")
     views = (texture, u, v)

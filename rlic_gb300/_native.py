@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
+import weakref
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().with_name("librlic_gb300.so")
@@ -88,6 +89,9 @@ SIGNATURES: dict[str, tuple[list, object]] = {
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
+    "rlic_release_cached_memory": ([], _INT),
+    "rlic_host_buffer_alloc": ([_SZ], _P),
+    "rlic_host_buffer_free": ([_P], None),
 }
 
 
@@ -150,6 +154,27 @@ def check(code: int) -> None:
         if code == RLIC_ERR_OUT_OF_MEMORY:
             raise MemoryError(f"rlic_gb300: {msg}")
         raise NativeLibraryError(f"rlic_gb300 error {code}: {msg}", code)
+
+
+def pinned_empty(shape: tuple, dtype) -> "np.ndarray":
+    """A new numpy array in a page-locked block from the library's host cache.
+
+    The block returns to the cache when the array (and every view of it) is
+    garbage-collected.  Falls back to np.empty when no block can be had.
+    """
+    import numpy as np
+
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    L = lib()
+    ptr = L.rlic_host_buffer_alloc(max(nbytes, 1))
+    if not ptr:
+        return np.empty(shape, dtype=dtype)
+    buf = (ctypes.c_char * max(nbytes, 1)).from_address(ptr)
+    free = L.rlic_host_buffer_free
+    weakref.finalize(buf, free, ctypes.c_void_p(ptr))
+    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    return arr
 
 
 def launch_count() -> int:

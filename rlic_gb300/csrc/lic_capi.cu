@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -121,6 +122,61 @@ void touch_pages(void* p, size_t bytes) {
     for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
     work(0);
     for (auto& th : pool) th.join();
+}
+
+// Scratch of calls that allocate (NULL workspace, host-memory calls) comes
+// from a stream-ordered pool owned by this library, one per device, that
+// keeps freed memory for the next call instead of returning it to the driver
+// at every synchronisation (the default pool's behaviour, which made every
+// call map its scratch afresh).  rlic_release_cached_memory() trims it.
+cudaMemPool_t library_pool(cudaError_t* err) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= 64) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        *err = cudaMemPoolCreate(&pool, &props);
+        if (*err != cudaSuccess) return nullptr;
+        uint64_t keep = UINT64_MAX;
+        *err = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (*err != cudaSuccess) return nullptr;
+        pools[dev] = pool;
+    }
+    return pools[dev];
+}
+
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
+    cudaError_t e = cudaSuccess;
+    cudaMemPool_t pool = library_pool(&e);
+    if (!pool) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, stream);
+}
+
+// Cache of page-locked host buffers for results handed to Python: a result
+// written into pinned memory needs no page faults and no staging copy, and a
+// buffer the caller has dropped is reused by the next call of the same size.
+struct HostBufferCache {
+    std::mutex mu;
+    std::multimap<size_t, void*> free_blocks;  // size -> block
+    std::map<void*, size_t> sizes;             // every block handed out
+    size_t cached_bytes = 0;
+};
+
+HostBufferCache& host_cache() {
+    static HostBufferCache* c = new HostBufferCache();  // lives until exit
+    return *c;
 }
 
 Variant make_variant(unsigned flags, int uv_mode) {
@@ -261,7 +317,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         unsigned char* ws = static_cast<unsigned char*>(workspace);
         bool owned = false;
         if (ws == nullptr) {
-            RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&ws), wl.total, stream));
+            RLIC_CUDA_TRY(scratch_alloc(reinterpret_cast<void**>(&ws), wl.total, stream));
             owned = true;
         } else {
             if (workspace_bytes_ < wl.total)
@@ -307,7 +363,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
     const size_t a_img = align_up(n * sizeof(T));
     const size_t total = (direct ? 2 : 4) * a_img + wl.total + kAlign;
     unsigned char* d = nullptr;
-    RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d), total, stream));
+    RLIC_CUDA_TRY(scratch_alloc(reinterpret_cast<void**>(&d), total, stream));
     T* d_tex = reinterpret_cast<T*>(d);
     T* d_out = reinterpret_cast<T*>(d + a_img);  // device ping-pong / result buffer
     T* d_u = direct ? const_cast<T*>(u) : reinterpret_cast<T*>(d + 2 * a_img);
@@ -387,7 +443,7 @@ int trace_cells_impl(const T* u, const T* v, int64_t ny, int64_t nx, int64_t kle
     const size_t a_cells = align_up(size_t(npix) * size_t(klen - 1) * sizeof(int64_t));
     const size_t total = a_uv + (host ? 2 * a_img + a_pix + a_cells : 0);
     unsigned char* d = nullptr;
-    RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d), total, stream));
+    RLIC_CUDA_TRY(scratch_alloc(reinterpret_cast<void**>(&d), total, stream));
     void* uv = d;
     auto body = [&]() -> int {
         const T* du = u;
@@ -537,7 +593,7 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
     unsigned char* ws = static_cast<unsigned char*>(workspace);
     bool owned = false;
     if (ws == nullptr) {
-        RLIC_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&ws), wl.total, stream));
+        RLIC_CUDA_TRY(scratch_alloc(reinterpret_cast<void**>(&ws), wl.total, stream));
         owned = true;
     } else {
         if (workspace_bytes_ < wl.total)
@@ -1014,5 +1070,68 @@ int rlic_set_block_shape(int block_x, int block_y) {
 }
 
 uint64_t rlic_kernel_launch_count(void) { return rlic::launches(); }
+
+void* rlic_host_buffer_alloc(size_t bytes) {
+    g_last_error.clear();
+    if (bytes == 0) bytes = 1;
+    auto& c = host_cache();
+    {
+        std::lock_guard<std::mutex> lock(c.mu);
+        auto it = c.free_blocks.find(bytes);
+        if (it != c.free_blocks.end()) {
+            void* p = it->second;
+            c.free_blocks.erase(it);
+            c.cached_bytes -= bytes;
+            return p;
+        }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaHostAlloc(&p, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        cuda_fail(e, "cudaHostAlloc");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(c.mu);
+    c.sizes[p] = bytes;
+    return p;
+}
+
+void rlic_host_buffer_free(void* p) {
+    if (!p) return;
+    auto& c = host_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto it = c.sizes.find(p);
+    if (it == c.sizes.end()) return;
+    c.free_blocks.emplace(it->second, p);
+    c.cached_bytes += it->second;
+    // keep at most 4 GiB of idle pinned memory
+    while (c.cached_bytes > (size_t(4) << 30) && !c.free_blocks.empty()) {
+        auto victim = std::prev(c.free_blocks.end());
+        c.cached_bytes -= victim->first;
+        c.sizes.erase(victim->second);
+        cudaFreeHost(victim->second);
+        c.free_blocks.erase(victim);
+    }
+}
+
+int rlic_release_cached_memory(void) {
+    g_last_error.clear();
+    {
+        auto& c = host_cache();
+        std::lock_guard<std::mutex> lock(c.mu);
+        for (auto& kv : c.free_blocks) {
+            c.sizes.erase(kv.second);
+            cudaFreeHost(kv.second);
+        }
+        c.free_blocks.clear();
+        c.cached_bytes = 0;
+    }
+    cudaError_t e = cudaSuccess;
+    cudaMemPool_t pool = library_pool(&e);
+    if (!pool) return cuda_fail(e, "cudaMemPoolCreate");
+    RLIC_CUDA_TRY(cudaDeviceSynchronize());
+    RLIC_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return RLIC_OK;
+}
 
 }  // extern "C"
