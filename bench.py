@@ -422,7 +422,10 @@ def run_gb300(args, dist: Dist) -> None:
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
     kw = dict(kernel=host["kernel"], uv_mode="polarization",
               boundaries={"x": "periodic", "y": "closed"}, iterations=ITERS)
-    rlic_gb300.convolve(host["texture"], host["u"], host["v"], **kw)
+    # warm-up as timed: each result is held while the next call runs, so the
+    # pinned result cache holds two buffers before timing starts
+    for _ in range(max(3, args.warmup)):
+        res = rlic_gb300.convolve(host["texture"], host["u"], host["v"], **kw)
     dist.barrier()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -540,6 +543,9 @@ def run_readme(args) -> None:
     steps = max(args.steps, 50)
     ms = _time_calls(call, steps, args.warmup, stream)
     samples = n * n * klen
+    for _ in range(max(3, args.warmup)):
+        res = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                                  boundaries="periodic")
     t0 = time.perf_counter()
     for _ in range(steps):
         rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], boundaries="periodic")

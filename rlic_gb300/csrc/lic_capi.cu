@@ -157,6 +157,35 @@ cudaMemPool_t library_pool(cudaError_t* err) {
     return pools[dev];
 }
 
+#ifndef RLIC_HOST_CHUNKS
+#define RLIC_HOST_CHUNKS 8
+#endif
+
+// A non-blocking stream per device for the uploads of host-memory calls, at
+// the greatest priority: the block scheduler then gives the upload kernels
+// the SM slots that the traced pass's blocks free, instead of queueing them
+// behind the whole pass.
+cudaStream_t aux_stream(cudaError_t* err) {
+    static std::mutex mu;
+    static cudaStream_t streams[64] = {};
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= 64) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!streams[dev]) {
+        int least = 0, greatest = 0;
+        *err = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (*err != cudaSuccess) return nullptr;
+        *err = cudaStreamCreateWithPriority(&streams[dev], cudaStreamNonBlocking, greatest);
+        if (*err != cudaSuccess) return nullptr;
+    }
+    return streams[dev];
+}
+
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
     cudaError_t e = cudaSuccess;
     cudaMemPool_t pool = library_pool(&e);
@@ -376,39 +405,146 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         if (!prefaulted) touch_pages(out, n * sizeof(T));
         prefaulted = true;
     };
+    // The inputs cross to the device in row chunks on an auxiliary stream,
+    // and the first pass starts on the tile rows whose rows and halo (klen/2
+    // rows, wrapped across a periodic edge) have arrived, so the upload
+    // overlaps the traced pass.
+    std::vector<cudaEvent_t> events;
+    cudaStream_t aux = nullptr;
     auto body = [&]() -> int {
-        if (strided) {
-            RLIC_CUDA_TRY(rlic::launch_gather_strided(texture, st[0], st[1], d_tex, ny, nx, stream));
-            RLIC_CUDA_TRY(rlic::launch_pack_strided(u, st[2], st[3], v, st[4], st[5],
-                                                    ws + wl.uv, ny, nx, stream));
-        } else {
-            RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex, texture, n * sizeof(T), cudaMemcpyHostToDevice,
-                                          stream));
-        }
-        if (!direct) {
-            RLIC_CUDA_TRY(cudaMemcpyAsync(d_u, u, n * sizeof(T), cudaMemcpyHostToDevice, stream));
-            RLIC_CUDA_TRY(cudaMemcpyAsync(d_v, v, n * sizeof(T), cudaMemcpyHostToDevice, stream));
-        }
         RLIC_CUDA_TRY(cudaMemcpyAsync(d_kernel, kernel, size_t(klen) * sizeof(T),
                                       cudaMemcpyHostToDevice, stream));
+        cudaError_t e = cudaSuccess;
+        aux = aux_stream(&e);
+        if (!aux) return cuda_fail(e, "cudaStreamCreate");
+        const int64_t R = klen / 2;
+        // up to RLIC_HOST_CHUNKS chunks of at least max(2R, 64) rows, for
+        // images of 4 Mpx and more
+        const int nchunks =
+            n < (size_t(1) << 22)
+                ? 1
+                : int(std::min<int64_t>(RLIC_HOST_CHUNKS,
+                                        std::max<int64_t>(1, ny / std::max<int64_t>(2 * R, 64))));
+        const int64_t rows_per = (ny + nchunks - 1) / nchunks;
+        const bool wraps_y = bnd[2] == RLIC_BOUNDARY_PERIODIC || bnd[3] == RLIC_BOUNDARY_PERIODIC;
+        std::vector<int> order;
+        if (wraps_y && nchunks > 1) order.push_back(nchunks - 1);
+        for (int c = 0; c < nchunks; ++c)
+            if (!(wraps_y && nchunks > 1 && c == nchunks - 1)) order.push_back(c);
+        std::vector<int> arrival(nchunks, 0);
+        for (int k = 0; k < nchunks; ++k) arrival[order[k]] = k;
+        events.resize(nchunks + 1, nullptr);
+        for (auto& ev : events) RLIC_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        // the scratch was allocated stream-ordered on `stream`
+        RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
+        RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
+        unsigned char* uvb = ws + wl.uv;
+        const bool cache = use_path_cache(iterations, klen, flags);
+        const Shape sh = make_shape(ny, nx, bnd);
+        const LaunchConfig lc = launch_config();
+        const int64_t tiles_x = (nx + lc.block_x - 1) / lc.block_x;
+        const int64_t tile_rows = (ny + lc.block_y - 1) / lc.block_y;
+        // arrival position after which each tile row has its rows and halo
+        std::vector<int> need(size_t(tile_rows), 0);
+        for (int64_t tr = 0; tr < tile_rows; ++tr) {
+            const int64_t lo = tr * lc.block_y - R;
+            const int64_t hi = std::min(ny, (tr + 1) * lc.block_y) - 1 + R;
+            for (int c = 0; c < nchunks; ++c) {
+                const int64_t c0 = c * rows_per, c1 = std::min(ny, c0 + rows_per);
+                bool hit = false;
+                if (wraps_y && hi - lo + 1 >= ny) {
+                    hit = true;
+                } else if (wraps_y) {  // rows lo..hi modulo ny
+                    for (int64_t shift = -ny; shift <= ny && !hit; shift += ny)
+                        hit = std::max(lo, c0 + shift) <= std::min(hi, c1 - 1 + shift);
+                } else {
+                    hit = std::max<int64_t>(lo, c0) <= std::min<int64_t>(hi, c1 - 1);
+                }
+                if (hit && c0 < c1) need[tr] = std::max(need[tr], arrival[c]);
+            }
+        }
+        uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
+        T* tmp = reinterpret_cast<T*>(ws + wl.tmp);
+        T* final_dst = direct ? out : d_out;
+        auto dst_of = [&](int64_t it) -> T* {
+            if (it + 1 == iterations) return final_dst;
+            return ((iterations - 1 - it) % 2 == 0) ? d_out : tmp;
+        };
+        if (iterations == 1) prefault();
+        const int mode = cache ? rlic::kPassSampleRecord : rlic::kPassSample;
+        for (int k = 0; k < nchunks; ++k) {
+            const int64_t r0 = order[k] * rows_per, r1 = std::min(ny, r0 + rows_per);
+            if (r0 < r1) {
+                const size_t off = size_t(r0) * size_t(nx), cnt = size_t(r1 - r0) * size_t(nx);
+                void* uv_rows = uvb + off * 2 * sizeof(T);
+                if (strided || direct) {  // kernels reading the caller's memory: no host stall
+                    RLIC_CUDA_TRY(rlic::launch_gather_strided(texture + r0 * st[0], st[0], st[1],
+                                                              d_tex + off, r1 - r0, nx, aux));
+                    RLIC_CUDA_TRY(rlic::launch_pack_strided(u + r0 * st[2], st[2], st[3],
+                                                            v + r0 * st[4], st[4], st[5],
+                                                            uv_rows, r1 - r0, nx, aux));
+                } else {
+                    RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex + off, texture + off, cnt * sizeof(T),
+                                                  cudaMemcpyHostToDevice, aux));
+                    RLIC_CUDA_TRY(cudaMemcpyAsync(d_u + off, u + off, cnt * sizeof(T),
+                                                  cudaMemcpyHostToDevice, aux));
+                    RLIC_CUDA_TRY(cudaMemcpyAsync(d_v + off, v + off, cnt * sizeof(T),
+                                                  cudaMemcpyHostToDevice, aux));
+                    RLIC_CUDA_TRY(rlic::launch_pack(d_u + off, d_v + off, uv_rows, int64_t(cnt), aux));
+                }
+            }
+            RLIC_CUDA_TRY(cudaEventRecord(events[k], aux));
+            // first pass over the tile rows this arrival completes, by runs
+            bool waited = false;
+            for (int64_t tr = 0; tr < tile_rows;) {
+                if (need[tr] != k) {
+                    ++tr;
+                    continue;
+                }
+                int64_t tr_end = tr + 1;
+                while (tr_end < tile_rows && need[tr_end] == k) ++tr_end;
+                if (!waited) RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[k], 0));
+                waited = true;
+                LaunchConfig part = lc;
+                part.tile_begin = tr * tiles_x;
+                part.tile_count = (tr_end - tr) * tiles_x;
+                RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen), sh,
+                                                part, dst_of(0), codes, stream));
+                tr = tr_end;
+            }
+        }
+        RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks - 1], 0));
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
             RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
-        int r = run_device<T>(d_tex, d_u, d_v, ny, nx, d_kernel, klen, var, bnd, iterations,
-                              d_out, ws, flags, stream, prefault, direct ? out : nullptr,
-                              strided);
-        if (r) return r;
+        const T* src = dst_of(0);
+        for (int64_t it = 1; it < iterations; ++it) {
+            if (it + 1 == iterations) prefault();
+            T* dst = dst_of(it);
+            if (cache) {
+                RLIC_CUDA_TRY(rlic::launch_gather(var.fma, src, codes, d_kernel, int(klen), sh,
+                                                  lc, dst, stream));
+            } else {
+                RLIC_CUDA_TRY(rlic::launch_pass(var, rlic::kPassSample, src, uvb, d_kernel,
+                                                int(klen), sh, lc, dst, codes, stream));
+            }
+            src = dst;
+        }
         prefault();
         if (!direct)
             RLIC_CUDA_TRY(cudaMemcpyAsync(out, d_out, n * sizeof(T), cudaMemcpyDeviceToHost, stream));
         return RLIC_OK;
     };
     rc = body();
+    // an upload still queued after a failure must end before the scratch is released
+    if (rc != RLIC_OK && aux) cudaStreamSynchronize(aux);
     unsigned negative = 0;
     cudaError_t ec = cudaSuccess;
     if (rc == RLIC_OK && (flags & RLIC_FLAG_CHECK_TEXTURE))
         ec = cudaMemcpyAsync(&negative, d_flag, sizeof(unsigned), cudaMemcpyDeviceToHost, stream);
     cudaError_t ef = cudaFreeAsync(d, stream);
     cudaError_t es = cudaStreamSynchronize(stream);
+    for (auto ev : events)
+        if (ev) cudaEventDestroy(ev);
     if (rc) return rc;
     if (ec != cudaSuccess) return cuda_fail(ec, "cudaMemcpyAsync");
     if (ef != cudaSuccess) return cuda_fail(ef, "cudaFreeAsync");

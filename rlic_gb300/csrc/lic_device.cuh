@@ -71,6 +71,50 @@ __device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
     return r;
 }
 
+// Predicates of the streamline step.  GB300 executes FP64 instructions,
+// comparisons included, at a small fraction of its FP32 rate, and the
+// float64 trace is bound by that pipe; for float64 these predicates read the
+// IEEE-754 bit patterns with integer instructions instead, with the same
+// results as the comparisons they replace.  float32 keeps plain comparisons.
+constexpr uint64_t kMagMask64 = 0x7FFFFFFFFFFFFFFFull;
+constexpr uint64_t kInfBits64 = 0x7FF0000000000000ull;
+__device__ __forceinline__ uint64_t bits_of(double x) { return uint64_t(__double_as_longlong(x)); }
+
+// x == 0 (either sign)
+__device__ __forceinline__ bool is_zero(float x) { return x == 0.f; }
+__device__ __forceinline__ bool is_zero(double x) { return (bits_of(x) & kMagMask64) == 0; }
+// isnan(x)
+__device__ __forceinline__ bool is_nan(float x) { return isnan(x); }
+__device__ __forceinline__ bool is_nan(double x) { return (bits_of(x) & kMagMask64) > kInfBits64; }
+// x >= 0 for x not NaN (true for -0.0)
+__device__ __forceinline__ bool nonneg(float x) { return x >= 0.f; }
+__device__ __forceinline__ bool nonneg(double x) {
+    const uint64_t b = bits_of(x);
+    return (b >> 63) == 0 || (b & kMagMask64) == 0;
+}
+// a < b for a, b with the sign bit clear (|.| results: magnitudes, +inf, NaN).
+// Such bit patterns order as unsigned integers the way the values do, NaN
+// above +inf; a NaN on either side gives false, as the comparison.
+__device__ __forceinline__ bool less_mag(float a, float b) { return a < b; }
+__device__ __forceinline__ bool less_mag(double a, double b) {
+    return bits_of(a) < bits_of(b) && bits_of(b) <= kInfBits64;
+}
+// add_rn(p, q) < 0.  The rounded sum has the sign of the exact sum: a nonzero
+// sum of two floating-point numbers never rounds to zero (a sum that
+// underflows is exact), an exact zero rounds to +0 (-0 only from -0 + -0,
+// which is not below 0), and overflow keeps the sign.  So the sum is
+// negative when both operands are negative and not both zero, or when the
+// negative operand has the larger magnitude; NaN operands and inf + -inf
+// (NaN) give false.
+__device__ __forceinline__ bool sum_negative(float p, float q) { return add_rn(p, q) < 0.f; }
+__device__ __forceinline__ bool sum_negative(double p, double q) {
+    const uint64_t bp = bits_of(p), bq = bits_of(q);
+    const uint64_t mp = bp & kMagMask64, mq = bq & kMagMask64;
+    const bool np = (bp >> 63) != 0, nq = (bq >> 63) != 0;
+    const bool neg = np ? (nq ? ((mp | mq) != 0) : (mp > mq)) : (nq && mq > mp);
+    return neg && mp <= kInfBits64 && mq <= kInfBits64;
+}
+
 // Accumulation of one kernel-weighted sample: `mul_add` in the default build
 // (src/lib.rs:357-360, 380-383), a rounded product then a rounded sum without
 // the `fma` feature (src/lib.rs:353-356, 376-379).
@@ -106,13 +150,13 @@ __device__ __forceinline__ T abs_quotient(T a, T b) {
 #if RLIC_QUOTIENT_GUARD == 0
     return abs_(div_rn(a, b));
 #elif RLIC_QUOTIENT_GUARD == 1
-    const bool a0 = (a == T(0));
+    const bool a0 = is_zero(a);
     const T q = abs_(div_rn(a0 ? T(1) : a, b));
-    return a0 ? ((b == T(0)) ? T(NAN) : T(0)) : q;
+    return a0 ? (is_zero(b) ? T(NAN) : T(0)) : q;
 #else
-    const bool a0 = (a == T(0));
-    const bool a0n = !(a < T(0) || a > T(0));  // zero or NaN
-    const bool b0 = (b == T(0));
+    const bool a0 = is_zero(a);
+    const bool a0n = a0 || is_nan(a);
+    const bool b0 = is_zero(b);
     const T q = abs_(div_rn((a0 | b0) ? T(1) : a, b0 ? T(1) : b));
     return b0 ? (a0n ? T(NAN) : T(INFINITY)) : (a0 ? T(0) : q);
 #endif
@@ -121,7 +165,7 @@ __device__ __forceinline__ T abs_quotient(T a, T b) {
 // Signed quotient a / b, for the branchy variant (b nonzero and not NaN).
 template <typename T>
 __device__ __forceinline__ T signed_quotient(T a, T b) {
-    const bool a0 = (a == T(0));
+    const bool a0 = is_zero(a);
     const T q = div_rn(a0 ? T(1) : a, b);
     return a0 ? ((signbit(a) != signbit(b)) ? T(-0.0) : T(0.0)) : q;
 }
@@ -242,7 +286,7 @@ __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
 template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
                                             const Geometry<I>& g) {
-    const bool still = (u == T(0)) & (v == T(0));
+    const bool still = is_zero(u) & is_zero(v);
     // A still lane keeps its state whatever the times are; giving it unit
     // velocities keeps its divisions on the fast path (a division by zero
     // takes the slow one) and its lane in step with the warp.
@@ -250,25 +294,27 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     const T sv = still ? T(1) : v;
     T tx, ty;
     times_to_next_pixel<T, FMA, BRANCHLESS>(su, sv, fx, fy, tx, ty);
-    const bool xstep = tx < ty;
+    // the branchless times are magnitudes (|.|, +inf or NaN): less_mag applies
+    const bool xstep = BRANCHLESS ? less_mag(tx, ty) : (tx < ty);
     const T t = xstep ? tx : ty;
     // the orthogonal update of either branch (update_state, src/lib.rs:225-232):
-    // an x step moves fy by t * v, a y step moves fx by t * u; both are
-    // computed and the branch keeps one
+    // an x step moves fy by t * v, a y step moves fx by t * u.  float32
+    // computes both in one packed instruction and keeps one; float64 computes
+    // only the one kept.
     T cx, cy;
     if constexpr (FMA && sizeof(T) == 4) {
         const float2 c = fma2_rn(make_float2(t, t), make_float2(su, sv), make_float2(fx, fy));
         cx = c.x;
         cy = c.y;
-    } else if constexpr (FMA) {
-        cx = fma_rn(t, su, fx);
-        cy = fma_rn(t, sv, fy);
     } else {
-        cx = add_rn(fx, mul_rn(t, su));
-        cy = add_rn(fy, mul_rn(t, sv));
+        const T vo = xstep ? sv : su;
+        const T fo = xstep ? fy : fx;
+        const T o = FMA ? fma_rn(t, vo, fo) : add_rn(fo, mul_rn(t, vo));
+        cx = o;
+        cy = o;
     }
     const T vpar = xstep ? su : sv;
-    const bool up = vpar >= T(0);
+    const bool up = nonneg(vpar);
     const T fpar = up ? T(0) : T(1);
     const T nfx = xstep ? fpar : cx;
     const T nfy = xstep ? cy : fpar;
@@ -333,16 +379,16 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
                                            const T* __restrict__ tex, uint32_t& code) {
     const auto p = __ldg(uv + st.cell);
     T pu = p.x, pv = p.y;
-    if (isnan(pu) || isnan(pv)) return false;
+    if (is_nan(pu) || is_nan(pv)) return false;
     if constexpr (POL) {
-        T dot;
+        bool flip;
         if constexpr (sizeof(T) == 4) {
             const float2 pr = mul2_rn(make_float2(pu, pv), make_float2(st.lu, st.lv));
-            dot = add_rn(pr.x, pr.y);
+            flip = sum_negative(pr.x, pr.y);
         } else {
-            dot = add_rn(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
+            flip = sum_negative(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
         }
-        if (dot < T(0)) {
+        if (flip) {
             pu = -pu;
             pv = -pv;
         }

@@ -75,6 +75,7 @@ struct TileGrid {
     I tiles_x, ntiles;
     int bx, by;
     int radius;  // max cells a streamline can move away from its pixel
+    I tile_base; // first tile of this launch (traced passes)
 };
 
 template <typename I>
@@ -150,7 +151,7 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
         __syncthreads();
     }
     const T wmid = (MODE != kRecordOnly) ? __ldg(kernel + kmid) : T(0);
-    const I tile = I(blockIdx.x);
+    const I tile = tg.tile_base + I(blockIdx.x);
     const I ti = tile / tg.tiles_x;
     const I tj = tile - ti * tg.tiles_x;
     const I i = ti * tg.by + I(threadIdx.y);
@@ -372,38 +373,141 @@ lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
 // from the caller's host memory.  A zero stride re-reads the same elements,
 // which then come from cache.
 
+// ------------------------------------------------ host-memory uploads --
+//
+// Kernels that read the caller's host arrays in place (pageable-memory
+// access over NVLink-C2C).  Those reads are latency-bound: a small grid with
+// several independent loads per thread in flight reaches the link's
+// bandwidth, and leaves the other SMs to the traced pass that runs on the
+// rows already uploaded.  RLIC_UPLOAD_CTAS bounds the grid; every thread
+// keeps kUploadUnroll loads in flight.
+
+#ifndef RLIC_UPLOAD_CTAS
+#define RLIC_UPLOAD_CTAS 32
+#endif
+constexpr int kUploadUnroll = 8;
+
+// dst[i * nx + j] = src[i * s0 + j * s1]
+template <typename T>
+__global__ void gather_strided_kernel(const T* __restrict__ src, int64_t s0, int64_t s1,
+                                      T* __restrict__ dst, int64_t ny, int64_t nx) {
+    const int64_t span = int64_t(blockDim.x) * kUploadUnroll;
+    for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
+        for (int64_t j0 = int64_t(blockIdx.x) * span + threadIdx.x; j0 < nx;
+             j0 += int64_t(gridDim.x) * span) {
+            T r[kUploadUnroll];
+#pragma unroll
+            for (int k = 0; k < kUploadUnroll; ++k) {
+                const int64_t j = j0 + int64_t(k) * blockDim.x;
+                if (j < nx) r[k] = src[i * s0 + j * s1];
+            }
+#pragma unroll
+            for (int k = 0; k < kUploadUnroll; ++k) {
+                const int64_t j = j0 + int64_t(k) * blockDim.x;
+                if (j < nx) dst[i * nx + j] = r[k];
+            }
+        }
+    }
+}
+
+// uv[i * nx + j] = (u[i * su0 + j * su1], v[i * sv0 + j * sv1])
 template <typename T>
 __global__ void pack_uv_strided_kernel(const T* __restrict__ u, int64_t su0, int64_t su1,
                                        const T* __restrict__ v, int64_t sv0, int64_t sv1,
                                        typename Vec2<T>::type* __restrict__ uv, int64_t ny,
                                        int64_t nx) {
+    constexpr int U = kUploadUnroll / 2;  // two loads per element
+    const int64_t span = int64_t(blockDim.x) * U;
     for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
-        for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nx;
-             j += int64_t(gridDim.x) * blockDim.x) {
-            typename Vec2<T>::type p;
-            p.x = u[i * su0 + j * su1];
-            p.y = v[i * sv0 + j * sv1];
-            uv[i * nx + j] = p;
+        for (int64_t j0 = int64_t(blockIdx.x) * span + threadIdx.x; j0 < nx;
+             j0 += int64_t(gridDim.x) * span) {
+            typename Vec2<T>::type r[U];
+#pragma unroll
+            for (int k = 0; k < U; ++k) {
+                const int64_t j = j0 + int64_t(k) * blockDim.x;
+                if (j < nx) {
+                    r[k].x = u[i * su0 + j * su1];
+                    r[k].y = v[i * sv0 + j * sv1];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < U; ++k) {
+                const int64_t j = j0 + int64_t(k) * blockDim.x;
+                if (j < nx) uv[i * nx + j] = r[k];
+            }
         }
     }
 }
 
+// Contiguous rows with 16-byte aligned starts: plain 16-byte vector copies
+// (T only tags the instantiation of each translation unit).
 template <typename T>
-__global__ void gather_strided_kernel(const T* __restrict__ src, int64_t s0, int64_t s1,
-                                      T* __restrict__ dst, int64_t ny, int64_t nx) {
-    for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
-        for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < nx;
-             j += int64_t(gridDim.x) * blockDim.x)
-            dst[i * nx + j] = src[i * s0 + j * s1];
+__global__ void copy_vec16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                  int64_t nvec) {
+    const int64_t span = int64_t(blockDim.x) * kUploadUnroll;
+    for (int64_t b = int64_t(blockIdx.x) * span + threadIdx.x; b < nvec;
+         b += int64_t(gridDim.x) * span) {
+        uint4 r[kUploadUnroll];
+#pragma unroll
+        for (int k = 0; k < kUploadUnroll; ++k) {
+            const int64_t q = b + int64_t(k) * blockDim.x;
+            if (q < nvec) r[k] = src[q];
+        }
+#pragma unroll
+        for (int k = 0; k < kUploadUnroll; ++k) {
+            const int64_t q = b + int64_t(k) * blockDim.x;
+            if (q < nvec) dst[q] = r[k];
+        }
     }
 }
 
-inline dim3 rows_grid(int64_t ny, int64_t nx) {
-    int64_t gx = (nx + 255) / 256;
-    if (gx > 64) gx = 64;
-    int64_t gy = ny < 65535 ? ny : 65535;
-    return dim3(unsigned(gx < 1 ? 1 : gx), unsigned(gy < 1 ? 1 : gy));
+// Contiguous u, v with 16-byte aligned rows: 16-byte vectors of u and of v
+// interleaved into two 16-byte vectors of (u, v) pairs.  ELEM_WORDS is the
+// element size in 32-bit words (1: float, 2: double).
+template <int ELEM_WORDS>
+__global__ void pack_vec16_kernel(const uint4* __restrict__ u, const uint4* __restrict__ v,
+                                  uint4* __restrict__ uv, int64_t nvec) {
+    constexpr int U = kUploadUnroll / 2;
+    const int64_t span = int64_t(blockDim.x) * U;
+    for (int64_t b = int64_t(blockIdx.x) * span + threadIdx.x; b < nvec;
+         b += int64_t(gridDim.x) * span) {
+        uint4 a[U], c[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const int64_t q = b + int64_t(k) * blockDim.x;
+            if (q < nvec) {
+                a[k] = u[q];
+                c[k] = v[q];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const int64_t q = b + int64_t(k) * blockDim.x;
+            if (q < nvec) {
+                if constexpr (ELEM_WORDS == 1) {
+                    uv[2 * q] = make_uint4(a[k].x, c[k].x, a[k].y, c[k].y);
+                    uv[2 * q + 1] = make_uint4(a[k].z, c[k].z, a[k].w, c[k].w);
+                } else {
+                    uv[2 * q] = make_uint4(a[k].x, a[k].y, c[k].x, c[k].y);
+                    uv[2 * q + 1] = make_uint4(a[k].z, a[k].w, c[k].z, c[k].w);
+                }
+            }
+        }
+    }
 }
+
+// Grid of an upload over ny rows of nx elements, `per_thread` elements per
+// thread per round, at most RLIC_UPLOAD_CTAS CTAs of 256 threads.
+inline dim3 upload_grid(int64_t ny, int64_t nx, int per_thread) {
+    const int64_t span = 256 * int64_t(per_thread);
+    int64_t gx = (nx + span - 1) / span;
+    gx = gx < 1 ? 1 : (gx > RLIC_UPLOAD_CTAS ? RLIC_UPLOAD_CTAS : gx);
+    int64_t gy = RLIC_UPLOAD_CTAS / gx;
+    gy = gy < 1 ? 1 : (gy > ny ? ny : gy);
+    return dim3(unsigned(gx), unsigned(gy < 1 ? 1 : gy));
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 // --------------------------------------------------------- input checks --
 
@@ -502,6 +606,7 @@ TileGrid<I> make_tiles(const Shape& sh, const LaunchConfig& lc, int klen) {
     tg.tiles_x = I(tiles_of(sh.nx, lc.block_x));
     tg.ntiles = tg.tiles_x * I(tiles_of(sh.ny, lc.block_y));
     tg.radius = klen / 2;
+    tg.tile_base = I(lc.tile_begin);
     return tg;
 }
 
@@ -569,7 +674,9 @@ cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int 
             cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         if (e != cudaSuccess) return e;
     }
-    kfn<<<unsigned(tg.ntiles), dim3(lc.block_x, lc.block_y), smem, stream>>>(
+    const int64_t count = lc.tile_count ? lc.tile_count : int64_t(tg.ntiles) - lc.tile_begin;
+    if (count <= 0) return cudaSuccess;
+    kfn<<<unsigned(count), dim3(lc.block_x, lc.block_y), smem, stream>>>(
         tex_in, static_cast<const typename Vec2<T>::type*>(uv), kernel, klen, g, tg, tex_out,
         codes, cl);
     count_launch();
@@ -669,20 +776,42 @@ inline unsigned stream_blocks(int64_t n) {
     return unsigned(blocks < 1 ? 1 : blocks);
 }
 
+// Rows [0, ny) of strided u, v into the packed field.  Contiguous rows with
+// 16-byte aligned starts take the vector kernel.
 template <typename T>
 cudaError_t launch_pack_strided_t(const T* u, int64_t su0, int64_t su1, const T* v, int64_t sv0,
                                   int64_t sv1, void* uv, int64_t ny, int64_t nx,
                                   cudaStream_t stream) {
-    pack_uv_strided_kernel<T><<<rows_grid(ny, nx), 256, 0, stream>>>(
-        u, su0, su1, v, sv0, sv1, static_cast<typename Vec2<T>::type*>(uv), ny, nx);
+    const int64_t per_vec = 16 / int64_t(sizeof(T));
+    if (su1 == 1 && sv1 == 1 && su0 == nx && sv0 == nx && nx % per_vec == 0 && aligned16(u) &&
+        aligned16(v) && aligned16(uv)) {
+        const int64_t nvec = ny * nx / per_vec;
+        const dim3 grid = upload_grid(1, nvec, kUploadUnroll / 2);
+        pack_vec16_kernel<int(sizeof(T) / 4)><<<grid.x, 256, 0, stream>>>(
+            reinterpret_cast<const uint4*>(u), reinterpret_cast<const uint4*>(v),
+            static_cast<uint4*>(uv), nvec);
+    } else {
+        pack_uv_strided_kernel<T><<<upload_grid(ny, nx, kUploadUnroll / 2), 256, 0, stream>>>(
+            u, su0, su1, v, sv0, sv1, static_cast<typename Vec2<T>::type*>(uv), ny, nx);
+    }
     count_launch();
     return cudaGetLastError();
 }
 
+// Rows [0, ny) of a strided array into a contiguous one.
 template <typename T>
 cudaError_t launch_gather_strided_t(const T* src, int64_t s0, int64_t s1, T* dst, int64_t ny,
                                     int64_t nx, cudaStream_t stream) {
-    gather_strided_kernel<T><<<rows_grid(ny, nx), 256, 0, stream>>>(src, s0, s1, dst, ny, nx);
+    const int64_t per_vec = 16 / int64_t(sizeof(T));
+    if (s1 == 1 && s0 == nx && nx % per_vec == 0 && aligned16(src) && aligned16(dst)) {
+        const int64_t nvec = ny * nx / per_vec;
+        const dim3 grid = upload_grid(1, nvec, kUploadUnroll);
+        copy_vec16_kernel<T><<<grid.x, 256, 0, stream>>>(reinterpret_cast<const uint4*>(src),
+                                                         reinterpret_cast<uint4*>(dst), nvec);
+    } else {
+        gather_strided_kernel<T><<<upload_grid(ny, nx, kUploadUnroll), 256, 0, stream>>>(
+            src, s0, s1, dst, ny, nx);
+    }
     count_launch();
     return cudaGetLastError();
 }

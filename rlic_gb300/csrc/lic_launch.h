@@ -29,6 +29,10 @@ struct Shape {
 // CTA shape in pixels.
 struct LaunchConfig {
     int block_x, block_y;
+    // traced passes only: launch the tiles [tile_begin, tile_begin +
+    // tile_count) of the row-major tile grid (tile_count 0: all tiles)
+    int64_t tile_begin = 0;
+    int64_t tile_count = 0;
 };
 
 // What a traced pass does per step: sample the texture, sample and record the

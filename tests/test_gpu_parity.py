@@ -321,14 +321,17 @@ def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
     u, v = np.ascontiguousarray(c["u"]), np.ascontiguousarray(c["v"])
+    # texture check + pack + traced pass + 2 replays, plus the texture upload
+    # as a gather kernel where the device reads host memory in place (else a
+    # copy-engine copy); one row chunk at this size
+    want = 6 if _native.lib().rlic_host_direct_access() else 5
     rlic_gb300.convolve(c["texture"], u, v, kernel=c["kernel"], iterations=3)
-    # texture check + pack + traced pass + 2 replays
-    assert _native.launch_count() - before == 5
+    assert _native.launch_count() - before == want
     before = _native.launch_count()
+    # broadcast u, v: read in place where the device reaches host memory,
+    # else made contiguous and copied
     rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], iterations=3)
-    # broadcast u, v: read in place (strided gather + strided pack) where the
-    # device reaches host memory, else copied (plain pack)
-    assert _native.launch_count() - before == (6 if _native.lib().rlic_host_direct_access() else 5)
+    assert _native.launch_count() - before == want
 
 
 def test_device_entry_points_with_workspace(oracle) -> None:
@@ -417,6 +420,10 @@ def test_host_path_without_direct_access(tmp_path) -> None:
         "out = rlic_gb300.convolve(c['texture'], c['u'], c['v'], kernel=c['kernel'],\n"
         "                          boundaries='periodic', iterations=3)\n"
         f"np.save({str(tmp_path / 'out.npy')!r}, out)\n"
+        "c = readme_case(n=2100, dtype=np.float32, seed=5)\n"
+        "out = rlic_gb300.convolve(c['texture'], c['u'], c['v'], kernel=c['kernel'],\n"
+        "                          boundaries='periodic', iterations=2)\n"
+        f"np.save({str(tmp_path / 'big.npy')!r}, out)\n"
     )
     env = dict(__import__("os").environ, RLIC_NO_HOST_DIRECT="1")
     subprocess.run([sys.executable, str(script)], check=True, env=env, timeout=300)
@@ -424,6 +431,39 @@ def test_host_path_without_direct_access(tmp_path) -> None:
     want = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
                                boundaries="periodic", iterations=3)
     assert_bitwise(np.load(tmp_path / "out.npy"), want)
+    # 4.4 Mpx: uploaded in row chunks by copy-engine copies
+    c = readme_case(n=2100, dtype=np.float32, seed=5)
+    want = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                               boundaries="periodic", iterations=2)
+    assert_bitwise(np.load(tmp_path / "big.npy"), want)
+
+
+@pytest.mark.parametrize("bnd, klen, iterations", [
+    ({"x": "periodic", "y": "closed"}, 65, 5),
+    ("periodic", 129, 3),
+    ({"x": "closed", "y": "periodic"}, 33, 1),
+    ("closed", 9, 2),
+])
+def test_host_path_row_chunks(bnd, klen, iterations) -> None:
+    """Host arrays of 4 Mpx and more go up in row chunks, with the traced pass
+    started per group of tile rows as their rows and halo arrive (across the
+    seam for a periodic y axis): same bits as the device-resident path,
+    contiguous and strided, on a ragged row count."""
+    import torch
+
+    rng = np.random.default_rng(klen)
+    ny, nx = 2101, 2050
+    u, v = _field(rng, ny, nx, np.float32, "specials")
+    tex = rng.random((ny, nx), dtype=np.float32)
+    k = np.hanning(klen).astype(np.float32)
+    kw = dict(uv_mode="polarization", boundaries=bnd, iterations=iterations)
+    want = rlic_gb300.convolve(torch.from_numpy(tex).cuda(), torch.from_numpy(u).cuda(),
+                               torch.from_numpy(v).cuda(), kernel=torch.from_numpy(k).cuda(),
+                               **kw).cpu().numpy()
+    assert_bitwise(rlic_gb300.convolve(tex, u, v, kernel=k, **kw), want)
+    # the same arrays read through transposed views of their transposes
+    tt, ut, vt = (np.ascontiguousarray(a.T).T for a in (tex, u, v))
+    assert_bitwise(rlic_gb300.convolve(tt, ut, vt, kernel=k, **kw), want)
 
 
 def test_strided_views_read_in_place(oracle) -> None:
