@@ -214,6 +214,65 @@ __device__ __forceinline__ void times_to_next_pixel(T u, T v, T fx, T fy, T& tx,
     }
 }
 
+// The branchless numerator fma(1 + signum(v), 0.5 - f, f) of
+// time_to_next_pixel (src/lib.rs:168-179), before its division.
+template <typename T, bool FMA>
+__device__ __forceinline__ T time_numerator(T vel, T frac) {
+    const T s = signbit(vel) ? T(0) : T(2);
+    const T d = sub_rn(T(0.5), frac);
+    return FMA ? fma_rn(s, d, frac) : add_rn(mul_rn(s, d), frac);
+}
+
+// float64 step choice with one division where two are not needed.
+//
+// A step compares tx = |ax / u| with ty = |ay / v| (both rounded), then uses
+// only the chosen one.  The float64 division is the bulk of the FP64 work
+// of a step, so the comparison is settled first, when it provably can be,
+// from the cross products |ax|*|v| and |ay|*|u| (tx < ty exactly when the
+// first is the smaller, up to the rounding of the quotients):
+//
+//   * every operand is truncated to float32 from its bit pattern (integer
+//     instructions): x' <= |x| < x' (1 + 2^-23);
+//   * the float32 products p1 = x'y' carry a further 2^-24 rounding, so
+//     p1 < p2 (1 - 2^-16) implies |ax||v| < |ay||u| (1 - 2^-17): the exact
+//     quotients differ by far more than one unit in the last place, hence
+//     so do the rounded ones, and tx < ty; symmetrically p1 > p2 (1 + 2^-16)
+//     implies tx > ty;
+//   * the screen runs only when u, v and the nonzero numerators are normal
+//     with binary exponents in [-60, 60], so that x', the products and the
+//     quotients stay normal and finite;
+//   * a zero numerator needs no division: |0 / u| = 0 for u nonzero, so
+//     tx < ty exactly when ax is zero and ay is not, and the time is 0.
+//
+// Returns false when the screen cannot decide (operands out of range, or
+// products within 2^-16 of each other); the caller then divides both.
+__device__ __forceinline__ bool screen_in_range(uint32_t hi) {
+    const uint32_t e = (hi >> 20) & 0x7FFu;  // biased exponent
+    return e - (1023u - 60u) <= 120u;
+}
+__device__ __forceinline__ float truncate_to_f32(double x) {
+    // |x| with 23 mantissa bits kept, for exponents in [-60, 60]
+    const uint64_t b = bits_of(x);
+    const uint32_t hi = uint32_t(b >> 32), lo = uint32_t(b);
+    const uint32_t e = ((hi >> 20) & 0x7FFu) - (1023u - 127u);
+    return __uint_as_float((e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ bool screen_step(double ax, double ay, double u, double v,
+                                            bool& xstep) {
+    const bool ax0 = is_zero(ax), ay0 = is_zero(ay);
+    const bool in_range = screen_in_range(uint32_t(bits_of(u) >> 32)) &&
+                          screen_in_range(uint32_t(bits_of(v) >> 32)) &&
+                          (ax0 || screen_in_range(uint32_t(bits_of(ax) >> 32))) &&
+                          (ay0 || screen_in_range(uint32_t(bits_of(ay) >> 32)));
+    const float p1 = __fmul_rn(truncate_to_f32(ax), truncate_to_f32(v));
+    const float p2 = __fmul_rn(truncate_to_f32(ay), truncate_to_f32(u));
+    const bool lt = p1 < __fmul_rn(p2, 1.0f - 0x1p-16f);
+    const bool gt = p1 > __fmul_rn(p2, 1.0f + 0x1p-16f);
+    const bool any0 = ax0 || ay0;
+    xstep = any0 ? (ax0 && !ay0) : lt;
+    return in_range && (any0 || lt || gt);
+}
+
 // One image axis with its two boundary rules (BoundaryPair, src/lib.rs:70-96),
 // pre-resolved: a coordinate that stepped to -1 becomes `lo_to`, one that
 // stepped to `size` becomes `hi_to` (closed: clamp; periodic: wrap).  The
@@ -292,11 +351,28 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     // takes the slow one) and its lane in step with the warp.
     const T su = still ? T(1) : u;
     const T sv = still ? T(1) : v;
-    T tx, ty;
-    times_to_next_pixel<T, FMA, BRANCHLESS>(su, sv, fx, fy, tx, ty);
-    // the branchless times are magnitudes (|.|, +inf or NaN): less_mag applies
-    const bool xstep = BRANCHLESS ? less_mag(tx, ty) : (tx < ty);
-    const T t = xstep ? tx : ty;
+    bool xstep;
+    T t;
+    if constexpr (BRANCHLESS && sizeof(T) == 8) {
+        // one division when the screen settles the comparison, else both
+        const T ax = time_numerator<T, FMA>(su, fx);
+        const T ay = time_numerator<T, FMA>(sv, fy);
+        const bool settled = screen_step(ax, ay, su, sv, xstep);
+        const bool first_x = !settled || xstep;
+        const T q = abs_quotient(first_x ? ax : ay, first_x ? su : sv);
+        t = q;
+        if (!settled) {
+            const T ty = abs_quotient(ay, sv);
+            xstep = less_mag(q, ty);
+            t = xstep ? q : ty;
+        }
+    } else {
+        T tx, ty;
+        times_to_next_pixel<T, FMA, BRANCHLESS>(su, sv, fx, fy, tx, ty);
+        // the branchless times are magnitudes (|.|, +inf or NaN): less_mag applies
+        xstep = BRANCHLESS ? less_mag(tx, ty) : (tx < ty);
+        t = xstep ? tx : ty;
+    }
     // the orthogonal update of either branch (update_state, src/lib.rs:225-232):
     // an x step moves fy by t * v, a y step moves fx by t * u.  float32
     // computes both in one packed instruction and keeps one; float64 computes

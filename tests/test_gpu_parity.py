@@ -177,6 +177,41 @@ def test_random_fields(oracle, dtype, uv_mode, bnd, kind) -> None:
 
 
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("uv_mode", ["velocity", "polarization"])
+def test_float64_near_ties_and_exponent_edges(oracle, variant, uv_mode) -> None:
+    """float64 steps settle tx < ty from float32 cross products when they are
+    2^-16 apart or more, and divide both times otherwise.  Fields with
+    |u| = |v| (1 + e) for e around that margin and down to one ulp, and
+    components at the edges of the screened exponent range (2^-61 .. 2^-59,
+    2^59 .. 2^61), must still give the oracle's cells and bits."""
+    rng = np.random.default_rng(7 + variant)
+    ny, nx = 43, 57
+    v = rng.uniform(0.2, 2.0, (ny, nx)) * rng.choice([-1.0, 1.0], (ny, nx))
+    eps = rng.choice([0.0, 2.0**-52, -(2.0**-52), 2.0**-40, 2.0**-20, -(2.0**-20), 2.0**-17,
+                      2.0**-16, -(2.0**-16), 2.0**-15, -(2.0**-15), 2.0**-10], (ny, nx))
+    u = v * (1.0 + eps) * rng.choice([-1.0, 1.0], (ny, nx))
+    m = rng.random((ny, nx))
+    scale = np.where(m < 0.1, 2.0**-60, np.where(m < 0.2, 2.0**60, 1.0))
+    scale *= np.where((m > 0.3) & (m < 0.35), 2.0**-61, 1.0)
+    scale *= np.where((m > 0.4) & (m < 0.45), 2.0**61, 1.0)
+    u, v = u * scale, v * scale
+    u[(m > 0.5) & (m < 0.53)] *= 2.0**-1000  # subnormal-range partners
+    tex = rng.random((ny, nx))
+    k = rng.random(33)
+    for bnd in ("closed", "periodic"):
+        want = oracle.convolve(tex, u, v, k, uv_mode=uv_mode, boundaries=bnd, iterations=2,
+                               variant=variant)
+        assert_bitwise(capi_convolve(tex, u, v, k, uv_mode, bnd, 2, variant), want)
+        assert_bitwise(capi_convolve(tex, u, v, k, uv_mode, bnd, 2, variant,
+                                     _native.RLIC_FLAG_NO_PATH_CACHE), want)
+        pix = np.arange(ny * nx)
+        np.testing.assert_array_equal(
+            capi_cells(u, v, 33, pix, uv_mode, bnd, variant),
+            oracle.paths(u, v, 33, pix, uv_mode=uv_mode, boundaries=bnd, variant=variant),
+        )
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_feature_variants(oracle, variant, dtype) -> None:
     rng = np.random.default_rng(100 + variant)
