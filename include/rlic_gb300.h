@@ -21,8 +21,10 @@
  *   - All pointers are CUDA device pointers unless RLIC_FLAG_HOST_MEMORY is
  *     set, in which case texture, u, v, kernel and out are host pointers and
  *     the call copies them to and from the device and returns after the result
- *     is back in `out`.  Without that flag the call is asynchronous on `stream`
- *     (a cudaStream_t; NULL means the legacy default stream).
+ *     is back in `out`; a NULL stream then means the calling thread's
+ *     per-thread default stream, so host-memory calls from several threads
+ *     overlap on the device.  Without that flag the call is asynchronous on
+ *     `stream` (a cudaStream_t; NULL means the legacy default stream).
  *   - `out` must not overlap any input.  Inputs are never written.
  *   - Return value: RLIC_OK or an RLIC_ERR_* code; rlic_last_error() then
  *     describes the failure (thread-local).
@@ -370,6 +372,17 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
  * or a divisor of 32).  Affects calls made after it on any thread.
  */
 RLIC_API int rlic_set_block_shape(int block_x, int block_y);
+
+/*
+ * Self-check of the float64 streamline step's screened division (no
+ * reference counterpart).  For nonzero a[i], b[i] with binary exponents in
+ * [-60, 60], sets certified[i] to 1 when the short division certified its
+ * result, and q[i] to its value of |a[i] / b[i]|, which must then equal
+ * the correctly rounded quotient.  Device pointers; asynchronous on
+ * `stream`.
+ */
+RLIC_API int rlic_check_quotients_f64(const double *a, const double *b, int64_t n, double *q,
+                                      int32_t *certified, void *stream);
 
 /*
  * Number of this library's kernels launched since load (all threads).  Lets

@@ -385,6 +385,10 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         std::memset(out, 0, n * sizeof(T));
         return RLIC_OK;
     }
+    // A host-memory call waits for its own work only: with no stream given
+    // it runs on the calling thread's per-thread stream, so that calls from
+    // several host threads overlap on the device.
+    if (stream == nullptr) stream = cudaStreamPerThread;
     const bool direct = host_direct_access();
     if (strided && !direct)
         return fail(RLIC_ERR_UNSUPPORTED,
@@ -1202,6 +1206,17 @@ int rlic_set_block_shape(int block_x, int block_y) {
         return fail(RLIC_ERR_INVALID_ARGUMENT, "block shape must have 1..256 threads");
     g_block_x.store(block_x);
     g_block_y.store(block_y);
+    return RLIC_OK;
+}
+
+int rlic_check_quotients_f64(const double* a, const double* b, int64_t n, double* q,
+                             int32_t* certified, void* stream) {
+    g_last_error.clear();
+    if (n < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "n must be >= 0");
+    if (n > 0 && (!a || !b || !q || !certified))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    RLIC_CUDA_TRY(rlic::launch_quotient_check(a, b, n, q, certified,
+                                              static_cast<cudaStream_t>(stream)));
     return RLIC_OK;
 }
 

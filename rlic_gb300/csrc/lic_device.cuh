@@ -37,7 +37,15 @@ __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
-__device__ __forceinline__ double abs_(double a) { return fabs(a); }
+// float64 |a| and -a clear or flip the sign bit with an integer instruction
+// (the same results as fabs and negation) and keep them off the FP64 pipe
+__device__ __forceinline__ double abs_(double a) {
+    return __longlong_as_double(__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ __forceinline__ float neg_(float a) { return -a; }
+__device__ __forceinline__ double neg_(double a) {
+    return __longlong_as_double(__double_as_longlong(a) ^ (1ll << 63));
+}
 
 // Packed pairs of float32 operations (sm_100-family f32x2 instructions): each
 // lane is rounded exactly as the scalar __fmaf_rn / __fsub_rn / __fmul_rn.
@@ -126,6 +134,16 @@ __device__ __forceinline__ T accumulate(T w, T x, T acc) {
         return add_rn(acc, mul_rn(w, x));
     }
 }
+
+// float32 steps: 1 = a lane whose velocity is zero (its state stays as it
+// is) leaves the step by a branch, which spares the other lanes the selects
+// that would keep its state (the float32 traced pass is bound by the ALU
+// pipe those selects use); 0 = it runs the step with stand-in velocities
+// and selects keep its state.  float64 steps always take the selects,
+// which measured faster there.
+#ifndef RLIC_STILL_BRANCH_F32
+#define RLIC_STILL_BRANCH_F32 1
+#endif
 
 // Which operands of the time divisions are routed around the division
 // sequence (see abs_quotient): 0 none, 1 zero numerators, 2 zero numerators
@@ -257,6 +275,62 @@ __device__ __forceinline__ float truncate_to_f32(double x) {
     const uint32_t e = ((hi >> 20) & 0x7FFu) - (1023u - 127u);
     return __uint_as_float((e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
 }
+// |a| / |b| rounded to nearest for nonzero a and b whose binary exponents
+// lie in [-60, 60] (the screened range), with 6 FP64 instructions instead of
+// a general division; returns false when it cannot certify the result (the
+// caller then divides with __ddiv_rn).  Methods: Newton-Raphson refinement
+// of a reciprocal from a float32 seed (Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 1990),
+// and the exact FMA remainder r = a - b q of a quotient within one ulp
+// (Boldo and Daumas, "Representable correcting terms for possibly
+// underflowing floating point operations", ARITH 2003), used here only as a
+// certificate:
+//
+//   y0 = rcp.approx(float32(|b|))          relative error < 2^-21
+//   y1 = y0 + y0 (1 - |b| y0)               relative error ~2^-42
+//   q0 = |a| y1;  q1 = q0 + y1 (|a| - |b| q0)
+//   r  = fma(-|b|, q1, |a|)
+//
+// q1 is the rounded quotient exactly when |a/b - q1| < ulp(q1)/2, i.e.
+// R = |r| / (|b| ulp(q1)) < 1/2 (q1 not a power of two, whose lower
+// neighbour is only half an ulp away: those are refused).  R is bounded
+// from r's and b's exponents and 23-bit mantissas with a 2^-16 margin; a
+// refused R (near a rounding tie, or q1 off by an ulp) falls back.  An
+// inexact r (q1 off by more than an ulp) has R near or above 1 and is
+// refused as well.  Every intermediate stays normal: |b| and |a| in
+// [2^-60, 2^61), quotients in (2^-121, 2^121), and a nonzero r is a
+// multiple of 2^-285.
+__device__ __forceinline__ double f32_to_f64_bits(float x) {
+    // exact widening of a normal positive float32 with integer instructions
+    const uint32_t b = __float_as_uint(x);
+    const uint64_t e = uint64_t(((b >> 23) & 0xFFu) + (1023u - 127u));
+    return __longlong_as_double(int64_t((e << 52) | (uint64_t(b & 0x7FFFFFu) << 29)));
+}
+__device__ __forceinline__ float mantissa_f32(double x) {
+    // the 23 leading fraction bits of x as a float32 in [1, 2)
+    const uint64_t b = bits_of(x);
+    return __uint_as_float((127u << 23) | uint32_t((b >> 29) & 0x7FFFFFu));
+}
+__device__ __forceinline__ bool quotient_screened(double a, double b, double& q) {
+    const double A = abs_(a), B = abs_(b);
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(truncate_to_f32(B)));
+    const double y0 = f32_to_f64_bits(r0);
+    const double y1 = fma_rn(y0, fma_rn(-B, y0, 1.0), y0);
+    const double q0 = mul_rn(A, y1);
+    const double q1 = fma_rn(fma_rn(-B, q0, A), y1, q0);
+    const double r = fma_rn(-B, q1, A);
+    q = q1;
+    const uint64_t bq = bits_of(q1), br = bits_of(r) & kMagMask64;
+    if ((bq & 0xFFFFFFFFFFFFFull) == 0) return false;  // power of two
+    if (br == 0) return true;                            // exact quotient
+    const int k = int(br >> 52) - int(bits_of(B) >> 52) - int(bq >> 52) + (1023 + 52);
+    if (k <= -3) return true;   // R < 2 * 2^-3
+    if (k >= 0) return false;   // R > 1/2
+    const float lhs = __fmul_rn(mantissa_f32(r), k == -1 ? 0.5f : 0.25f);
+    return lhs < __fmul_rn(mantissa_f32(B), 0.5f - 0x1p-17f);
+}
+
 __device__ __forceinline__ bool screen_step(double ax, double ay, double u, double v,
                                             bool& xstep) {
     const bool ax0 = is_zero(ax), ay0 = is_zero(ay);
@@ -346,6 +420,9 @@ template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
                                             const Geometry<I>& g) {
     const bool still = is_zero(u) & is_zero(v);
+    if constexpr (sizeof(T) == 4 && RLIC_STILL_BRANCH_F32) {
+        if (still) return 0u;  // the state stays as it is (src/lib.rs:242-244)
+    }
     // A still lane keeps its state whatever the times are; giving it unit
     // velocities keeps its divisions on the fast path (a division by zero
     // takes the slow one) and its lane in step with the warp.
@@ -359,12 +436,21 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
         const T ay = time_numerator<T, FMA>(sv, fy);
         const bool settled = screen_step(ax, ay, su, sv, xstep);
         const bool first_x = !settled || xstep;
-        const T q = abs_quotient(first_x ? ax : ay, first_x ? su : sv);
-        t = q;
-        if (!settled) {
-            const T ty = abs_quotient(ay, sv);
-            xstep = less_mag(q, ty);
-            t = xstep ? q : ty;
+        const T num = first_x ? ax : ay;
+        const T den = first_x ? su : sv;
+        // settled lanes: the screened division (a zero numerator gives 0)
+        const bool num0 = is_zero(num);
+        T q;
+        const bool certified = quotient_screened(num0 ? T(1) : num, den, q);
+        t = num0 ? T(0) : q;
+        if (!(settled && certified)) {  // rare: general divisions
+            const T q1 = abs_quotient(num, den);
+            t = q1;
+            if (!settled) {
+                const T ty = abs_quotient(ay, sv);
+                xstep = less_mag(q1, ty);
+                t = xstep ? q1 : ty;
+            }
         }
     } else {
         T tx, ty;
@@ -465,15 +551,15 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
             flip = sum_negative(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
         }
         if (flip) {
-            pu = -pu;
-            pv = -pv;
+            pu = neg_(pu);
+            pv = neg_(pv);
         }
         st.lu = pu;
         st.lv = pv;
     }
     if constexpr (BACKWARD) {
-        pu = -pu;
-        pv = -pv;
+        pu = neg_(pu);
+        pv = neg_(pv);
     }
     code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, g);
     if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, __ldg(tex + st.cell), acc);

@@ -98,6 +98,10 @@ cudaError_t launch_gather_lowp(int storage, const void* tex_in, const uint32_t* 
                                const Shape& sh, const LaunchConfig& lc, void* tex_out,
                                cudaStream_t stream);
 
+// Self-check of the screened float64 division (lic_kernels_f64.cu).
+cudaError_t launch_quotient_check(const double* a, const double* b, int64_t n, double* q,
+                                  int32_t* certified, cudaStream_t stream);
+
 #undef RLIC_DECLARE_LAUNCHERS
 
 }  // namespace rlic

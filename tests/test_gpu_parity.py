@@ -501,6 +501,28 @@ def test_host_path_row_chunks(bnd, klen, iterations) -> None:
     assert_bitwise(rlic_gb300.convolve(tt, ut, vt, kernel=k, **kw), want)
 
 
+def test_concurrent_host_calls_from_threads() -> None:
+    """The ctypes call releases the GIL and a host-memory call runs on its
+    thread's own stream: calls from several Python threads at once (large
+    enough to take the chunked upload) give each caller its own result."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    cases = [readme_case(n=2100, klen=k, dtype=np.float32, seed=s)
+             for s, k in ((1, 33), (2, 65), (3, 17), (4, 65))]
+    kw = dict(boundaries={"x": "periodic", "y": "closed"}, uv_mode="polarization",
+              iterations=3)
+
+    def run(c):
+        return rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], **kw)
+
+    want = [run(c) for c in cases]
+    with ThreadPoolExecutor(max_workers=4) as pool:
+        for _ in range(3):
+            got = list(pool.map(run, cases))
+            for g, w in zip(got, want):
+                assert_bitwise(g, w)
+
+
 def test_strided_views_read_in_place(oracle) -> None:
     """Broadcast, transposed, reversed and sliced numpy views give the bits of
     their contiguous copies (read in place where the device can reach host
