@@ -36,16 +36,33 @@ __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, 
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+// Bit patterns of float64 values moved through an opaque register move.  A
+// plain bit cast would let the compiler turn integer tests and sign-bit
+// edits back into FP64 compares, abs and negations, and GB300 runs FP64
+// instructions at a small fraction of its FP32 rate (see the predicates
+// below).
+__device__ __forceinline__ uint64_t bits_of(double x) {
+    uint64_t r;
+    asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+    return r;
+}
+__device__ __forceinline__ double from_bits(uint64_t b) {
+    double r;
+    asm("mov.b64 %0, %1;" : "=d"(r) : "l"(b));
+    return r;
+}
+
 __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
 // float64 |a| and -a clear or flip the sign bit with an integer instruction
 // (the same results as fabs and negation) and keep them off the FP64 pipe
 __device__ __forceinline__ double abs_(double a) {
-    return __longlong_as_double(__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll);
+    return from_bits(bits_of(a) & 0x7FFFFFFFFFFFFFFFull);
 }
 __device__ __forceinline__ float neg_(float a) { return -a; }
-__device__ __forceinline__ double neg_(double a) {
-    return __longlong_as_double(__double_as_longlong(a) ^ (1ll << 63));
-}
+__device__ __forceinline__ double neg_(double a) { return from_bits(bits_of(a) ^ (1ull << 63)); }
+// signbit for the numerator's 1 + signum(v) (exactly 0 or 2)
+__device__ __forceinline__ bool sign_set(float x) { return signbit(x); }
+__device__ __forceinline__ bool sign_set(double x) { return (bits_of(x) >> 63) != 0; }
 
 // Packed pairs of float32 operations (sm_100-family f32x2 instructions): each
 // lane is rounded exactly as the scalar __fmaf_rn / __fsub_rn / __fmul_rn.
@@ -86,7 +103,6 @@ __device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
 // results as the comparisons they replace.  float32 keeps plain comparisons.
 constexpr uint64_t kMagMask64 = 0x7FFFFFFFFFFFFFFFull;
 constexpr uint64_t kInfBits64 = 0x7FF0000000000000ull;
-__device__ __forceinline__ uint64_t bits_of(double x) { return uint64_t(__double_as_longlong(x)); }
 
 // x == 0 (either sign)
 __device__ __forceinline__ bool is_zero(float x) { return x == 0.f; }
@@ -199,7 +215,7 @@ __device__ __forceinline__ T signed_quotient(T a, T b) {
 template <typename T, bool FMA, bool BRANCHLESS>
 __device__ __forceinline__ T time_to_next_pixel(T vel, T frac) {
     if constexpr (BRANCHLESS) {
-        const T s = signbit(vel) ? T(0) : T(2);
+        const T s = sign_set(vel) ? T(0) : T(2);
         const T d = sub_rn(T(0.5), frac);
         T rem;
         if constexpr (FMA) {
@@ -236,7 +252,7 @@ __device__ __forceinline__ void times_to_next_pixel(T u, T v, T fx, T fy, T& tx,
 // time_to_next_pixel (src/lib.rs:168-179), before its division.
 template <typename T, bool FMA>
 __device__ __forceinline__ T time_numerator(T vel, T frac) {
-    const T s = signbit(vel) ? T(0) : T(2);
+    const T s = sign_set(vel) ? T(0) : T(2);
     const T d = sub_rn(T(0.5), frac);
     return FMA ? fma_rn(s, d, frac) : add_rn(mul_rn(s, d), frac);
 }
@@ -304,7 +320,7 @@ __device__ __forceinline__ double f32_to_f64_bits(float x) {
     // exact widening of a normal positive float32 with integer instructions
     const uint32_t b = __float_as_uint(x);
     const uint64_t e = uint64_t(((b >> 23) & 0xFFu) + (1023u - 127u));
-    return __longlong_as_double(int64_t((e << 52) | (uint64_t(b & 0x7FFFFFu) << 29)));
+    return from_bits((e << 52) | (uint64_t(b & 0x7FFFFFu) << 29));
 }
 __device__ __forceinline__ float mantissa_f32(double x) {
     // the 23 leading fraction bits of x as a float32 in [1, 2)
