@@ -67,13 +67,14 @@ def parse_args() -> argparse.Namespace:
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload",
-                   choices=["fourier", "readme", "precision", "adjoint", "batched"],
+                   choices=["fourier", "readme", "precision", "adjoint", "batched", "equalize"],
                    default="fourier",
                    help="fourier: the headline 8192^2 float32 case (default); readme: the "
                         "reference's README case, 256^2 float64; precision: 8192^2 float64, "
                         "K=129, 10 iterations, exact vs FP16/BF16 storage forms; adjoint: "
                         "1024^2 float32, K=33, 3 iterations, forward + backward; batched: 64 "
-                        "instances of sides 256-4096, K 17-129, 1-10 iterations")
+                        "instances of sides 256-4096, K 17-129, 1-10 iterations; equalize: "
+                        "histogram equalization of an 8192^2 float32 image")
     return p.parse_args()
 
 
@@ -673,6 +674,36 @@ def run_adjoint(args) -> None:
     }), flush=True)
 
 
+def run_equalize(args) -> None:
+    """Histogram equalization of an 8192^2 float32 LIC-like image (uniform^3,
+    seed 0), 256 bins: global, sliding tile (65 x 65 windows) and tile
+    interpolation (64 x 64 tiles), device-resident."""
+    import torch
+
+    from rlic_gb300 import equalize as E
+
+    n, nbins = args.size, 256
+    dev = torch.device("cuda", 0)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    x = torch.rand((n, n), generator=gen, device=dev, dtype=torch.float32) ** 3
+    stream = torch.cuda.current_stream(dev)
+    forms = {
+        "global": lambda: E.equalize_histogram(x, nbins),
+        "sliding_tile_65x65": lambda: E.equalize_histogram_sliding_tile(x, nbins, (65, 65)),
+        "tile_interpolation_64x64": lambda: E.equalize_histogram_tile_interpolation(
+            x, nbins, (64, 64)),
+    }
+    res = {}
+    for name, fn in forms.items():
+        ms = _time_calls(fn, max(3, min(args.steps, 10)), args.warmup, stream)
+        res[name] = {"ms": ms, "gpx_per_s": n * n / (ms / 1e3) / 1e9}
+    print(json.dumps({
+        "metric": "Gpixels/s", "unit": "Gpx/s", "workload": f"equalize_{n}x{n}_f32_bins{nbins}",
+        "value": res["global"]["gpx_per_s"], "dtype": "f32", "forms": res,
+        "note": "post-processing of the LIC output; no counterpart implemented in the reference",
+    }), flush=True)
+
+
 def run_batched(args) -> None:
     """64 instances (rlic_gb300.workloads.batch_case, seed 3): one batched call
     (and its CUDA-graph replay) against 64 sequential rlic_convolve_f32 calls."""
@@ -753,6 +784,8 @@ def main() -> None:
         run_precision(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "equalize":
+        run_equalize(args)
     elif args.workload == "batched":
         run_batched(args)
     else:

@@ -374,6 +374,38 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
 RLIC_API int rlic_set_block_shape(int block_x, int block_y);
 
 /*
+ * Histogram equalization of an ny x nx image (float32 or float64), the
+ * post-processing step commonly applied to LIC output.  The reference
+ * declares these operations in its native-module stubs
+ * (src/rlic/_core.pyi:30-57: equalize_histogram_*,
+ * equalize_histogram_sliding_tile_*, equalize_histogram_tile_interpolation_*)
+ * without implementing them; the definitions are this library's own
+ * (oracle/histogram.py states them):
+ *   - bins: nbins equal bins over [min, max] of the finite pixels;
+ *   - RLIC_EQUALIZE_GLOBAL: cumulative histogram / finite-pixel count;
+ *   - RLIC_EQUALIZE_SLIDING_TILE: the pixel's rank among the finite pixels
+ *     of the tile_y x tile_x window around it (clipped to the image);
+ *   - RLIC_EQUALIZE_TILE_INTERPOLATION: per-tile mappings (tiles of
+ *     tile_y x tile_x) blended bilinearly between the four nearest tile
+ *     centres.
+ * Non-finite pixels are returned unchanged.  nbins in [1, 2^24] (tile
+ * interpolation: at most 49152); tile_y, tile_x >= 1 for the tile
+ * strategies.  `flags` takes RLIC_FLAG_HOST_MEMORY only.  Device pointers
+ * are processed asynchronously on `stream`.
+ */
+#define RLIC_EQUALIZE_GLOBAL 0
+#define RLIC_EQUALIZE_SLIDING_TILE 1
+#define RLIC_EQUALIZE_TILE_INTERPOLATION 2
+RLIC_API int rlic_equalize_histogram_f32(const float *image, int64_t ny, int64_t nx,
+                                         int64_t nbins, int strategy, int64_t tile_y,
+                                         int64_t tile_x, float *out, void *stream,
+                                         unsigned flags);
+RLIC_API int rlic_equalize_histogram_f64(const double *image, int64_t ny, int64_t nx,
+                                         int64_t nbins, int strategy, int64_t tile_y,
+                                         int64_t tile_x, double *out, void *stream,
+                                         unsigned flags);
+
+/*
  * Self-check of the float64 streamline step's screened division (no
  * reference counterpart).  For nonzero a[i], b[i] with binary exponents in
  * [-60, 60], sets certified[i] to 1 when the short division certified its

@@ -1,4 +1,5 @@
-"""CPU oracle of rLIC's convolution (test infrastructure only).
+"""CPU oracle of rLIC's convolution, and the numpy definition of histogram
+equalization (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` use this package, as the checker; the product package

@@ -48,6 +48,7 @@ SOURCES = [
     "lic_kernels_f64.cu",
     "lic_lowp.cu",
     "lic_batch.cu",
+    "lic_equalize.cu",
 ]
 
 

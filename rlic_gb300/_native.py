@@ -88,6 +88,8 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_check_quotients_f64": ([_P, _P, _I64, _P, _P, _P], _INT),
+    "rlic_equalize_histogram_f32": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
+    "rlic_equalize_histogram_f64": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
     "rlic_release_cached_memory": ([], _INT),

@@ -23,6 +23,7 @@
 //               texture, so both forms give identical results.
 #include "../../include/rlic_gb300.h"
 #include "lic_batch.h"
+#include "lic_equalize.h"
 #include "lic_launch.h"
 
 #include <algorithm>
@@ -1014,6 +1015,59 @@ int convolve_noalloc_f32(const float* texture, const float* u, const float* v, i
                              bnd, iterations, out, ws, flags, static_cast<cudaStream_t>(stream_));
 }
 
+// Histogram equalization (lic_equalize.cu): validation, scratch, host copies.
+template <typename T>
+int equalize_impl(const T* image, int64_t ny, int64_t nx, int64_t nbins, int strategy,
+                  int64_t tile_y, int64_t tile_x, T* out, void* stream_, unsigned flags) {
+    g_last_error.clear();
+    if (ny < 0 || nx < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "negative image shape");
+    if (nbins < 1 || nbins > rlic::kEqualizeMaxBins)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "nbins must be in [1, 2^24]");
+    if (strategy != RLIC_EQUALIZE_GLOBAL && strategy != RLIC_EQUALIZE_SLIDING_TILE &&
+        strategy != RLIC_EQUALIZE_TILE_INTERPOLATION)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "unknown equalization strategy");
+    if (strategy != RLIC_EQUALIZE_GLOBAL && (tile_y < 1 || tile_x < 1))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "tile shape must be positive");
+    if (strategy == RLIC_EQUALIZE_TILE_INTERPOLATION && nbins > rlic::kEqualizeMaxTileBins)
+        return fail(RLIC_ERR_UNSUPPORTED, "tile interpolation takes at most 49152 bins");
+    if (flags & ~RLIC_FLAG_HOST_MEMORY)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "unknown flag bits for this entry point");
+    const size_t n = size_t(ny) * size_t(nx);
+    if (n == 0) return RLIC_OK;
+    if (!image || !out) return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    const bool host = flags & RLIC_FLAG_HOST_MEMORY;
+    if (host && stream == nullptr) stream = cudaStreamPerThread;
+    const size_t scratch = rlic::equalize_scratch_bytes(ny, nx, nbins, strategy, tile_y, tile_x,
+                                                        sizeof(T));
+    const size_t a_img = align_up(n * sizeof(T));
+    unsigned char* d = nullptr;
+    RLIC_CUDA_TRY(scratch_alloc(reinterpret_cast<void**>(&d), scratch + (host ? 2 * a_img : 0),
+                                stream));
+    const T* src = image;
+    T* dst = out;
+    cudaError_t e = cudaSuccess;
+    if (host) {
+        T* d_in = reinterpret_cast<T*>(d + scratch);
+        dst = reinterpret_cast<T*>(d + scratch + a_img);
+        e = cudaMemcpyAsync(d_in, image, n * sizeof(T), cudaMemcpyHostToDevice, stream);
+        src = d_in;
+    }
+    if (e == cudaSuccess)
+        e = rlic::launch_equalize(src, ny, nx, int(nbins), strategy, tile_y, tile_x, dst, d,
+                                  stream);
+    if (e == cudaSuccess && host)
+        e = cudaMemcpyAsync(out, dst, n * sizeof(T), cudaMemcpyDeviceToHost, stream);
+    const cudaError_t ef = cudaFreeAsync(d, stream);
+    if (host) {
+        const cudaError_t es = cudaStreamSynchronize(stream);
+        if (e == cudaSuccess) e = es;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "histogram equalization");
+    if (ef != cudaSuccess) return cuda_fail(ef, "cudaFreeAsync");
+    return RLIC_OK;
+}
+
 }  // namespace
 
 // -------------------------------------------------------------------- C ABI --
@@ -1283,6 +1337,20 @@ int rlic_release_cached_memory(void) {
     RLIC_CUDA_TRY(cudaDeviceSynchronize());
     RLIC_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
     return RLIC_OK;
+}
+
+int rlic_equalize_histogram_f32(const float* image, int64_t ny, int64_t nx, int64_t nbins,
+                                int strategy, int64_t tile_y, int64_t tile_x, float* out,
+                                void* stream, unsigned flags) {
+    return equalize_impl<float>(image, ny, nx, nbins, strategy, tile_y, tile_x, out, stream,
+                                flags);
+}
+
+int rlic_equalize_histogram_f64(const double* image, int64_t ny, int64_t nx, int64_t nbins,
+                                int strategy, int64_t tile_y, int64_t tile_x, double* out,
+                                void* stream, unsigned flags) {
+    return equalize_impl<double>(image, ny, nx, nbins, strategy, tile_y, tile_x, out, stream,
+                                 flags);
 }
 
 }  // extern "C"

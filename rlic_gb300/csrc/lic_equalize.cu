@@ -1,0 +1,452 @@
+// lic_equalize.cu -- histogram equalization of an image on the GPU.
+//
+// The reference declares equalize_histogram{,_sliding_tile,
+// _tile_interpolation}_{f32,f64} in its native-module stubs
+// (src/rlic/_core.pyi:30-57) without implementing them (README.md:19-23
+// points to the separate `ahe` package), so the definitions here are this
+// library's own; oracle/histogram.py states them in numpy and the GPU
+// results match it bit for bit.  Every step rounds once in the image's
+// dtype, in the order of that definition.
+//
+// Work, for an ny x nx image:
+//   1. finite min / max / count: one pass, block reductions, one atomic per
+//      block on order-preserving integer encodings;
+//   2. bin of every pixel (int32, -1 for non-finite);
+//   3a. global: shared-memory histograms per block, merged with atomics,
+//       one-block inclusive scan, then out = cdf[bin] / count;
+//   3b. tile interpolation: one CTA per tile builds its histogram in shared
+//       memory, scans it and writes the tile's mapping; each pixel then
+//       blends the mappings of its four nearest tile centres;
+//   3c. sliding tile: each pixel counts the bins <= its own in its window
+//       (reads through L1; neighbouring pixels share the window's lines).
+#include "../../include/rlic_gb300.h"
+#include "lic_equalize.h"
+#include "lic_launch.h"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rlic {
+namespace {
+
+// Order-preserving unsigned encodings of finite floats (for atomic min/max).
+__device__ __forceinline__ uint32_t order_key(float x) {
+    const uint32_t b = __float_as_uint(x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ float from_key(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+__device__ __forceinline__ double from_key(unsigned long long k) {
+    return __longlong_as_double(static_cast<long long>(
+        (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
+template <typename T> struct KeyOf;
+template <> struct KeyOf<float> { using type = uint32_t; };
+template <> struct KeyOf<double> { using type = unsigned long long; };
+
+template <typename T>
+struct Stats {
+    typename KeyOf<T>::type lo_key, hi_key;
+    unsigned long long count;
+};
+
+template <typename T> __device__ __forceinline__ T div_rn_(T a, T b);
+template <> __device__ __forceinline__ float div_rn_(float a, float b) { return __fdiv_rn(a, b); }
+template <> __device__ __forceinline__ double div_rn_(double a, double b) { return __ddiv_rn(a, b); }
+template <typename T> __device__ __forceinline__ T sub_rn_(T a, T b);
+template <> __device__ __forceinline__ float sub_rn_(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ double sub_rn_(double a, double b) { return __dsub_rn(a, b); }
+template <typename T> __device__ __forceinline__ T mul_rn_(T a, T b);
+template <> __device__ __forceinline__ float mul_rn_(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ double mul_rn_(double a, double b) { return __dmul_rn(a, b); }
+template <typename T> __device__ __forceinline__ T add_rn_(T a, T b);
+template <> __device__ __forceinline__ float add_rn_(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ double add_rn_(double a, double b) { return __dadd_rn(a, b); }
+// integer count -> T, rounded to nearest (as numpy's int64 -> float cast)
+template <typename T> __device__ __forceinline__ T from_count(unsigned long long c);
+template <> __device__ __forceinline__ float from_count(unsigned long long c) {
+    return __ull2float_rn(c);
+}
+template <> __device__ __forceinline__ double from_count(unsigned long long c) {
+    return __ull2double_rn(c);
+}
+
+template <typename T>
+__global__ void stats_init_kernel(Stats<T>* st) {
+    st->lo_key = ~typename KeyOf<T>::type(0);
+    st->hi_key = 0;
+    st->count = 0;
+}
+
+template <typename T>
+__global__ void minmax_kernel(const T* __restrict__ x, int64_t n, Stats<T>* st) {
+    using K = typename KeyOf<T>::type;
+    K lo = ~K(0), hi = K(0);
+    unsigned long long cnt = 0;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const T v = x[k];
+        if (isfinite(v)) {
+            const K key = order_key(v);
+            lo = key < lo ? key : lo;
+            hi = key > hi ? key : hi;
+            ++cnt;
+        }
+    }
+    __shared__ K s_lo[32], s_hi[32];
+    __shared__ unsigned long long s_cnt[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        const K olo = __shfl_down_sync(0xffffffffu, lo, off);
+        const K ohi = __shfl_down_sync(0xffffffffu, hi, off);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+        lo = olo < lo ? olo : lo;
+        hi = ohi > hi ? ohi : hi;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        s_lo[warp] = lo;
+        s_hi[warp] = hi;
+        s_cnt[warp] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < int(blockDim.x >> 5); ++w) {
+            lo = s_lo[w] < lo ? s_lo[w] : lo;
+            hi = s_hi[w] > hi ? s_hi[w] : hi;
+            cnt += s_cnt[w];
+        }
+        if (cnt) {
+            atomicMin(&st->lo_key, lo);
+            atomicMax(&st->hi_key, hi);
+            atomicAdd(&st->count, cnt);
+        }
+    }
+}
+
+// bin(p) as defined in oracle/histogram.py; -1 for non-finite pixels.
+template <typename T>
+__global__ void bins_kernel(const T* __restrict__ x, int64_t n, const Stats<T>* st, int nbins,
+                            int32_t* __restrict__ bins) {
+    const T lo = from_key(st->lo_key), hi = from_key(st->hi_key);
+    const T span = sub_rn_(hi, lo);
+    const bool spread = st->count > 0 && hi > lo && isfinite(span);
+    const T scale = spread ? div_rn_(T(nbins), span) : T(0);
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const T v = x[k];
+        int32_t b = -1;
+        if (isfinite(v)) {
+            b = 0;
+            if (spread) {
+                const T s = floor(mul_rn_(sub_rn_(v, lo), scale));
+                b = s >= T(nbins - 1) ? nbins - 1 : int32_t(s);
+            }
+        }
+        bins[k] = b;
+    }
+}
+
+// Global histogram: shared-memory counts per block when they fit.
+__global__ void hist_kernel(const int32_t* __restrict__ bins, int64_t n, int nbins,
+                            unsigned long long* __restrict__ hist, bool shared) {
+    extern __shared__ uint32_t s_hist[];
+    if (shared) {
+        for (int k = threadIdx.x; k < nbins; k += blockDim.x) s_hist[k] = 0u;
+        __syncthreads();
+    }
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const int32_t b = bins[k];
+        if (b >= 0) {
+            if (shared) {
+                atomicAdd(&s_hist[b], 1u);
+            } else {
+                atomicAdd(&hist[b], 1ull);
+            }
+        }
+    }
+    if (shared) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < nbins; k += blockDim.x)
+            if (s_hist[k]) atomicAdd(&hist[k], (unsigned long long)s_hist[k]);
+    }
+}
+
+// Inclusive scan of v[0..n) by one block of 1024 threads, in chunks.
+template <typename V>
+__device__ void block_inclusive_scan(V* v, int64_t n) {
+    __shared__ V s_part[1024];
+    __shared__ V s_carry;
+    if (threadIdx.x == 0) s_carry = V(0);
+    __syncthreads();
+    for (int64_t base = 0; base < n; base += blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        s_part[threadIdx.x] = k < n ? v[k] : V(0);
+        __syncthreads();
+        for (int off = 1; off < int(blockDim.x); off <<= 1) {
+            const V add = threadIdx.x >= unsigned(off) ? s_part[threadIdx.x - off] : V(0);
+            __syncthreads();
+            s_part[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (k < n) v[k] = s_part[threadIdx.x] + s_carry;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_carry += s_part[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+__global__ void scan_kernel(unsigned long long* hist, int nbins) {
+    block_inclusive_scan(hist, nbins);
+}
+
+template <typename T>
+__global__ void map_global_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins,
+                                  int64_t n, const unsigned long long* __restrict__ cdf,
+                                  const Stats<T>* st, T* __restrict__ out) {
+    const T count = from_count<T>(st->count);
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const int32_t b = bins[k];
+        out[k] = b >= 0 ? div_rn_(from_count<T>(cdf[b]), count) : x[k];
+    }
+}
+
+// One CTA per tile: histogram in shared memory, scan, mapping m_t(k).
+template <typename T>
+__global__ void tile_maps_kernel(const int32_t* __restrict__ bins, int64_t ny, int64_t nx,
+                                 int64_t th, int64_t tw, int64_t ntx, int nbins,
+                                 T* __restrict__ maps) {
+    extern __shared__ uint32_t s_cdf[];
+    __shared__ uint32_t s_n;
+    const int64_t t = blockIdx.x;
+    const int64_t a = t / ntx, c = t - a * ntx;
+    const int64_t r0 = a * th, r1 = (r0 + th < ny) ? r0 + th : ny;
+    const int64_t c0 = c * tw, c1 = (c0 + tw < nx) ? c0 + tw : nx;
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x) s_cdf[k] = 0u;
+    if (threadIdx.x == 0) s_n = 0u;
+    __syncthreads();
+    const int64_t w = c1 - c0, cells = (r1 - r0) * w;
+    uint32_t mine = 0;
+    for (int64_t q = threadIdx.x; q < cells; q += blockDim.x) {
+        const int64_t i = r0 + q / w, j = c0 + q % w;
+        const int32_t b = bins[i * nx + j];
+        if (b >= 0) {
+            atomicAdd(&s_cdf[b], 1u);
+            ++mine;
+        }
+    }
+    if (mine) atomicAdd(&s_n, mine);
+    __syncthreads();
+    block_inclusive_scan(s_cdf, nbins);
+    __syncthreads();
+    const uint32_t nt = s_n;
+    T* m = maps + t * nbins;
+    const T tn = from_count<T>(nt);
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x)
+        m[k] = nt ? div_rn_(from_count<T>(s_cdf[k]), tn) : T(0);
+}
+
+// Tile centre (r0 + r1 - 1) / 2 of tile a along an axis of n cells in tiles of t.
+template <typename T>
+__device__ __forceinline__ T tile_centre(int64_t a, int64_t t, int64_t n) {
+    const int64_t r0 = a * t, r1 = (r0 + t < n) ? r0 + t : n;
+    return div_rn_(T(r0 + r1 - 1), T(2));
+}
+
+// (a0, a1, f) of position i against the tile centres of one axis.
+template <typename T>
+__device__ __forceinline__ void interp_axis(int64_t i, int64_t t, int64_t n, int64_t nt,
+                                            int64_t& a0, int64_t& a1, T& f) {
+    const T pos = T(i);
+    const T first = tile_centre<T>(0, t, n), last = tile_centre<T>(nt - 1, t, n);
+    f = T(0);
+    if (!(pos > first)) {
+        a0 = a1 = 0;
+        return;
+    }
+    if (!(pos < last)) {
+        a0 = a1 = nt - 1;
+        return;
+    }
+    // the last centre <= i: centres of full tiles are a t + (t - 1) / 2
+    int64_t a = (2 * i - (t - 1)) / (2 * t);
+    if (a < 0) a = 0;
+    if (a > nt - 1) a = nt - 1;
+    while (a + 1 < nt && !(tile_centre<T>(a + 1, t, n) > pos)) ++a;
+    while (a > 0 && tile_centre<T>(a, t, n) > pos) --a;
+    a0 = a;
+    a1 = a + 1;
+    const T c0 = tile_centre<T>(a0, t, n), c1 = tile_centre<T>(a1, t, n);
+    f = div_rn_(sub_rn_(pos, c0), sub_rn_(c1, c0));
+}
+
+template <typename T>
+__device__ __forceinline__ T lerp_rn(T u, T w, T f) {
+    return add_rn_(u, mul_rn_(f, sub_rn_(w, u)));
+}
+
+template <typename T>
+__global__ void map_tiles_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins,
+                                 int64_t ny, int64_t nx, int64_t th, int64_t tw, int64_t nty,
+                                 int64_t ntx, int nbins, const T* __restrict__ maps,
+                                 T* __restrict__ out) {
+    const int64_t n = ny * nx;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const int32_t b = bins[k];
+        if (b < 0) {
+            out[k] = x[k];
+            continue;
+        }
+        const int64_t i = k / nx, j = k - i * nx;
+        int64_t ra0, ra1, ca0, ca1;
+        T fy, fx;
+        interp_axis<T>(i, th, ny, nty, ra0, ra1, fy);
+        interp_axis<T>(j, tw, nx, ntx, ca0, ca1, fx);
+        const T m00 = maps[(ra0 * ntx + ca0) * nbins + b];
+        const T m01 = maps[(ra0 * ntx + ca1) * nbins + b];
+        const T m10 = maps[(ra1 * ntx + ca0) * nbins + b];
+        const T m11 = maps[(ra1 * ntx + ca1) * nbins + b];
+        out[k] = lerp_rn(lerp_rn(m00, m01, fx), lerp_rn(m10, m11, fx), fy);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
+                                              const int32_t* __restrict__ bins, int64_t ny,
+                                              int64_t nx, int64_t th, int64_t tw, int64_t i,
+                                              int64_t j, T* __restrict__ out);
+
+// Sliding tile: rank of the pixel's bin within its window.
+template <typename T>
+__global__ void sliding_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins,
+                               int64_t ny, int64_t nx, int64_t th, int64_t tw,
+                               T* __restrict__ out) {
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= nx) return;
+    for (int64_t i = int64_t(blockIdx.y) * blockDim.y + threadIdx.y; i < ny;
+         i += int64_t(gridDim.y) * blockDim.y) {
+        sliding_pixel(x, bins, ny, nx, th, tw, i, j, out);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
+                                              const int32_t* __restrict__ bins, int64_t ny,
+                                              int64_t nx, int64_t th, int64_t tw, int64_t i,
+                                              int64_t j, T* __restrict__ out) {
+    const int64_t k = i * nx + j;
+    const int32_t b = bins[k];
+    if (b < 0) {
+        out[k] = x[k];
+        return;
+    }
+    const int64_t r0 = i - th / 2 < 0 ? 0 : i - th / 2;
+    const int64_t r1 = i - th / 2 + th > ny ? ny : i - th / 2 + th;
+    const int64_t c0 = j - tw / 2 < 0 ? 0 : j - tw / 2;
+    const int64_t c1 = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
+    unsigned long long below = 0, valid = 0;
+    for (int64_t r = r0; r < r1; ++r) {
+        const int32_t* row = bins + r * nx;
+        for (int64_t c = c0; c < c1; ++c) {
+            const int32_t q = __ldg(row + c);
+            valid += q >= 0;
+            below += (q >= 0) & (q <= b);
+        }
+    }
+    out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
+}
+
+unsigned grid_for(int64_t n) {
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    return unsigned(blocks < 1 ? 1 : blocks);
+}
+
+}  // namespace
+
+size_t equalize_scratch_bytes(int64_t ny, int64_t nx, int64_t nbins, int strategy,
+                              int64_t th, int64_t tw, size_t elem) {
+    const int64_t n = ny * nx;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t total = up(sizeof(Stats<double>)) + up(size_t(n) * sizeof(int32_t));
+    if (strategy == RLIC_EQUALIZE_GLOBAL) total += up(size_t(nbins) * 8);
+    if (strategy == RLIC_EQUALIZE_TILE_INTERPOLATION) {
+        const int64_t ntiles = ((ny + th - 1) / th) * ((nx + tw - 1) / tw);
+        total += up(size_t(ntiles) * size_t(nbins) * elem);
+    }
+    return total;
+}
+
+template <typename T>
+cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int strategy,
+                              int64_t th, int64_t tw, T* out, void* scratch,
+                              cudaStream_t stream) {
+    const int64_t n = ny * nx;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    Stats<T>* st = reinterpret_cast<Stats<T>*>(base);
+    int32_t* bins = reinterpret_cast<int32_t*>(base + up(sizeof(Stats<double>)));
+    unsigned char* rest = base + up(sizeof(Stats<double>)) + up(size_t(n) * sizeof(int32_t));
+    cudaError_t e = cudaSuccess;
+    stats_init_kernel<T><<<1, 1, 0, stream>>>(st);
+    count_launch();
+    minmax_kernel<T><<<grid_for(n), 256, 0, stream>>>(x, n, st);
+    count_launch();
+    bins_kernel<T><<<grid_for(n), 256, 0, stream>>>(x, n, st, nbins, bins);
+    count_launch();
+    if (strategy == RLIC_EQUALIZE_GLOBAL) {
+        unsigned long long* hist = reinterpret_cast<unsigned long long*>(rest);
+        e = cudaMemsetAsync(hist, 0, size_t(nbins) * 8, stream);
+        if (e != cudaSuccess) return e;
+        const bool shared = nbins <= 12288;
+        hist_kernel<<<grid_for(n), 256, shared ? size_t(nbins) * 4 : 0, stream>>>(
+            bins, n, nbins, hist, shared);
+        count_launch();
+        scan_kernel<<<1, 1024, 0, stream>>>(hist, nbins);
+        count_launch();
+        map_global_kernel<T><<<grid_for(n), 256, 0, stream>>>(x, bins, n, hist, st, out);
+        count_launch();
+    } else if (strategy == RLIC_EQUALIZE_TILE_INTERPOLATION) {
+        const int64_t nty = (ny + th - 1) / th, ntx = (nx + tw - 1) / tw;
+        T* maps = reinterpret_cast<T*>(rest);
+        const size_t smem = size_t(nbins) * 4;
+        auto kfn = tile_maps_kernel<T>;
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if (e != cudaSuccess) return e;
+        }
+        kfn<<<unsigned(nty * ntx), 1024, smem, stream>>>(bins, ny, nx, th, tw, ntx, nbins, maps);
+        count_launch();
+        map_tiles_kernel<T><<<grid_for(n), 256, 0, stream>>>(x, bins, ny, nx, th, tw, nty, ntx,
+                                                            nbins, maps, out);
+        count_launch();
+    } else {
+        const dim3 block(32, 8);
+        const int64_t gy = (ny + 7) / 8;
+        const dim3 grid(unsigned((nx + 31) / 32), unsigned(gy < 65535 ? gy : 65535));
+        sliding_kernel<T><<<grid, block, 0, stream>>>(x, bins, ny, nx, th, tw, out);
+        count_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_equalize(const float* x, int64_t ny, int64_t nx, int nbins, int strategy,
+                            int64_t th, int64_t tw, float* out, void* scratch,
+                            cudaStream_t stream) {
+    return launch_equalize_t<float>(x, ny, nx, nbins, strategy, th, tw, out, scratch, stream);
+}
+cudaError_t launch_equalize(const double* x, int64_t ny, int64_t nx, int nbins, int strategy,
+                            int64_t th, int64_t tw, double* out, void* scratch,
+                            cudaStream_t stream) {
+    return launch_equalize_t<double>(x, ny, nx, nbins, strategy, th, tw, out, scratch, stream);
+}
+
+}  // namespace rlic

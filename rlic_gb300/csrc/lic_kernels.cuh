@@ -42,10 +42,11 @@
 namespace rlic {
 
 // Minimum resident CTAs per SM for the float32 / 32-bit-index replay
-// kernel's register allocation (8: 32 registers, full occupancy; measured
-// fastest at 8192^2).  Wider types need more registers and keep fewer CTAs.
+// kernel's register allocation (6: 40 registers, 75% occupancy; measured
+// fastest at 8192^2, 7% ahead of 8 blocks of 32 registers, which spill).
+// Wider types need more registers and keep fewer CTAs.
 #ifndef RLIC_GATHER_MIN_BLOCKS
-#define RLIC_GATHER_MIN_BLOCKS 8
+#define RLIC_GATHER_MIN_BLOCKS 6
 #endif
 
 template <typename T> struct PassMinBlocks { static constexpr int value = 1; };
