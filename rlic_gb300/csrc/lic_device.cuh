@@ -257,6 +257,35 @@ __device__ __forceinline__ T time_numerator(T vel, T frac) {
     return FMA ? fma_rn(s, d, frac) : add_rn(mul_rn(s, d), frac);
 }
 
+// Axis of a trace's last move: before the first move both fractions are
+// 0.5; after a move along an axis, that axis's fraction is exactly 0 or 1
+// (update_state, src/lib.rs:217-223).
+constexpr int kLastNone = 0, kLastX = 1, kLastY = 2;
+
+// The numerator fma(1 + signum(v), 0.5 - f, f) for f exactly 0, 0.5 or 1,
+// without FP64 instructions: 0.5 for f = 0.5; for f in {0, 1} with
+// s = 1 + signum(v) in {0, 2}, s = 2 gives 1 - f and s = 0 gives f, all
+// exact (2 * 0.5 + 0 = 1, 2 * -0.5 + 1 = +0, 0 * x + f = f).  The product
+// and sum of the branchless build without `fma` give the same values.
+__device__ __forceinline__ double known_numerator(double vel, double frac, bool centre) {
+    const bool s2 = !sign_set(vel);
+    const bool one = (bits_of(frac) >> 52) == 0x3FFull;  // frac == 1.0 (else +0)
+    return centre ? 0.5 : ((s2 != one) ? 1.0 : 0.0);
+}
+
+// Both numerators of a float64 step, computing in FP64 only the one of the
+// axis whose fraction is not known exactly (the axis not moved last; x
+// before the first move, when both are 0.5).
+template <bool FMA>
+__device__ __forceinline__ void time_numerators(double u, double v, double fx, double fy,
+                                                int last, double& ax, double& ay) {
+    const bool gen_y = (last == kLastX);
+    const double g = time_numerator<double, FMA>(gen_y ? v : u, gen_y ? fy : fx);
+    const double k = known_numerator(gen_y ? u : v, gen_y ? fx : fy, last == kLastNone);
+    ax = gen_y ? k : g;
+    ay = gen_y ? g : k;
+}
+
 // float64 step choice with one division where two are not needed.
 //
 // A step compares tx = |ax / u| with ty = |ay / v| (both rounded), then uses
@@ -434,7 +463,7 @@ __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
 // Returns the step code (see above).
 template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
-                                            const Geometry<I>& g) {
+                                            int& last, const Geometry<I>& g) {
     const bool still = is_zero(u) & is_zero(v);
     if constexpr (sizeof(T) == 4 && RLIC_STILL_BRANCH_F32) {
         if (still) return 0u;  // the state stays as it is (src/lib.rs:242-244)
@@ -447,9 +476,10 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     bool xstep;
     T t;
     if constexpr (BRANCHLESS && sizeof(T) == 8) {
-        // one division when the screen settles the comparison, else both
-        const T ax = time_numerator<T, FMA>(su, fx);
-        const T ay = time_numerator<T, FMA>(sv, fy);
+        // one division when the screen settles the comparison, else both;
+        // one numerator computed in FP64 (see known_numerator)
+        T ax, ay;
+        time_numerators<FMA>(su, sv, fx, fy, last, ax, ay);
         const bool settled = screen_step(ax, ay, su, sv, xstep);
         const bool first_x = !settled || xstep;
         const T num = first_x ? ax : ay;
@@ -498,6 +528,7 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     const T nfy = xstep ? cy : fpar;
     fx = still ? fx : nfx;
     fy = still ? fy : nfy;
+    last = still ? last : (xstep ? kLastX : kLastY);
     if constexpr (!EDGE) {
         const I step = xstep ? I(1) : g.nx;
         cell += still ? I(0) : (up ? step : -step);
@@ -540,6 +571,7 @@ template <typename T, typename I>
 struct TraceState {
     T fx, fy;  // position inside the cell, starting at the centre (0.5, 0.5)
     T lu, lv;  // previous sample in polarization mode, starting at (0, 0)
+    int last;  // axis of the last move (kLastNone before the first)
     I cell, i, j;
 };
 
@@ -577,7 +609,8 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
         pu = neg_(pu);
         pv = neg_(pv);
     }
-    code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, g);
+    code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, st.last,
+                                             g);
     if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, __ldg(tex + st.cell), acc);
     return true;
 }
@@ -598,6 +631,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
                                            const T* __restrict__ tex, const T* w, int count,
                                            uint32_t* __restrict__ words, size_t stride) {
     TraceState<T, I> st;
+    st.last = kLastNone;
     st.fx = T(0.5);
     st.fy = T(0.5);
     st.lu = T(0);
@@ -644,6 +678,7 @@ __device__ __forceinline__ void walk_half(I i, I j, const Geometry<I>& g,
                                           const typename Vec2<T>::type* __restrict__ uv,
                                           int count, Rec rec) {
     TraceState<T, I> st;
+    st.last = kLastNone;
     st.fx = T(0.5);
     st.fy = T(0.5);
     st.lu = T(0);

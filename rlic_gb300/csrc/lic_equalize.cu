@@ -321,27 +321,28 @@ __global__ void map_tiles_kernel(const T* __restrict__ x, const int32_t* __restr
 template <typename T>
 __device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
                                               const int32_t* __restrict__ bins, int64_t ny,
-                                              int64_t nx, int64_t th, int64_t tw, int64_t i,
-                                              int64_t j, T* __restrict__ out);
+                                              int64_t nx, int64_t th, int64_t tw, bool all_finite,
+                                              int64_t i, int64_t j, T* __restrict__ out);
 
 // Sliding tile: rank of the pixel's bin within its window.
 template <typename T>
 __global__ void sliding_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins,
                                int64_t ny, int64_t nx, int64_t th, int64_t tw,
-                               T* __restrict__ out) {
+                               const Stats<T>* st, T* __restrict__ out) {
     const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= nx) return;
+    const bool all_finite = st->count == (unsigned long long)(ny * nx);
     for (int64_t i = int64_t(blockIdx.y) * blockDim.y + threadIdx.y; i < ny;
          i += int64_t(gridDim.y) * blockDim.y) {
-        sliding_pixel(x, bins, ny, nx, th, tw, i, j, out);
+        sliding_pixel(x, bins, ny, nx, th, tw, all_finite, i, j, out);
     }
 }
 
 template <typename T>
 __device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
                                               const int32_t* __restrict__ bins, int64_t ny,
-                                              int64_t nx, int64_t th, int64_t tw, int64_t i,
-                                              int64_t j, T* __restrict__ out) {
+                                              int64_t nx, int64_t th, int64_t tw, bool all_finite,
+                                              int64_t i, int64_t j, T* __restrict__ out) {
     const int64_t k = i * nx + j;
     const int32_t b = bins[k];
     if (b < 0) {
@@ -352,15 +353,18 @@ __device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
     const int64_t r1 = i - th / 2 + th > ny ? ny : i - th / 2 + th;
     const int64_t c0 = j - tw / 2 < 0 ? 0 : j - tw / 2;
     const int64_t c1 = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
-    unsigned long long below = 0, valid = 0;
+    // a non-finite cell holds -1, which as an unsigned value is above every
+    // bin: one unsigned compare counts the finite cells whose bin is <= b
+    const uint32_t ub = uint32_t(b);
+    const int w = int(c1 - c0);
+    uint32_t below = 0, invalid = 0;
     for (int64_t r = r0; r < r1; ++r) {
-        const int32_t* row = bins + r * nx;
-        for (int64_t c = c0; c < c1; ++c) {
-            const int32_t q = __ldg(row + c);
-            valid += q >= 0;
-            below += (q >= 0) & (q <= b);
-        }
+        const int32_t* row = bins + r * nx + c0;
+        for (int c = 0; c < w; ++c) below += uint32_t(__ldg(row + c)) <= ub;
+        if (!all_finite)
+            for (int c = 0; c < w; ++c) invalid += __ldg(row + c) < 0;
     }
+    const uint32_t valid = uint32_t((r1 - r0) * w) - invalid;
     out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
 }
 
@@ -432,7 +436,7 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
         const dim3 block(32, 8);
         const int64_t gy = (ny + 7) / 8;
         const dim3 grid(unsigned((nx + 31) / 32), unsigned(gy < 65535 ? gy : 65535));
-        sliding_kernel<T><<<grid, block, 0, stream>>>(x, bins, ny, nx, th, tw, out);
+        sliding_kernel<T><<<grid, block, 0, stream>>>(x, bins, ny, nx, th, tw, st, out);
         count_launch();
     }
     return cudaGetLastError();
