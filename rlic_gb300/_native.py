@@ -9,11 +9,15 @@ missing or cannot be loaded, every call that needs it raises
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
 import weakref
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().with_name("librlic_gb300.so")
+# the in-tree build, or another build of the same sources named by
+# RLIC_GB300_LIBRARY (for example one compiled with different tuning macros)
+LIB_PATH = Path(os.environ.get("RLIC_GB300_LIBRARY") or
+                Path(__file__).resolve().with_name("librlic_gb300.so"))
 
 RLIC_OK = 0
 RLIC_ERR_INVALID_ARGUMENT = 1

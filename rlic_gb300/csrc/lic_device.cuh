@@ -160,6 +160,12 @@ __device__ __forceinline__ T accumulate(T w, T x, T acc) {
 #ifndef RLIC_STILL_BRANCH_F32
 #define RLIC_STILL_BRANCH_F32 1
 #endif
+#ifndef RLIC_F32_FLIP_MUL
+#define RLIC_F32_FLIP_MUL 0
+#endif
+#ifndef RLIC_F32_STILL_SUM
+#define RLIC_F32_STILL_SUM 0
+#endif
 
 // Which operands of the time divisions are routed around the division
 // sequence (see abs_quotient): 0 none, 1 zero numerators, 2 zero numerators
@@ -187,6 +193,15 @@ __device__ __forceinline__ T abs_quotient(T a, T b) {
     const bool a0 = is_zero(a);
     const T q = abs_(div_rn(a0 ? T(1) : a, b));
     return a0 ? (is_zero(b) ? T(NAN) : T(0)) : q;
+#elif RLIC_QUOTIENT_GUARD == 3
+    // a zero numerator divides a small power of two instead (2^-24 for
+    // float32, 2^-53 for float64: the quotient stays finite for every
+    // nonzero b, subnormals included) and keeps q * 0: 0 for b nonzero,
+    // NaN for b zero (q = inf), as |0 / b|
+    const bool a0 = is_zero(a);
+    const T tiny = sizeof(T) == 4 ? T(0x1p-24) : T(0x1p-53);
+    const T q = abs_(div_rn(a0 ? tiny : a, b));
+    return a0 ? mul_rn(q, T(0)) : q;
 #else
     const bool a0 = is_zero(a);
     const bool a0n = a0 || is_nan(a);
@@ -464,7 +479,14 @@ __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
 template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
                                             int& last, const Geometry<I>& g) {
-    const bool still = is_zero(u) & is_zero(v);
+    bool still;
+    if constexpr (sizeof(T) == 4 && RLIC_F32_STILL_SUM) {
+        // |u| + |v| is zero exactly when both are (u, v are not NaN here, and
+        // a sum of two subnormals does not underflow to zero)
+        still = add_rn(abs_(u), abs_(v)) == T(0);
+    } else {
+        still = is_zero(u) & is_zero(v);
+    }
     if constexpr (sizeof(T) == 4 && RLIC_STILL_BRANCH_F32) {
         if (still) return 0u;  // the state stays as it is (src/lib.rs:242-244)
     }
@@ -598,7 +620,14 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
         } else {
             flip = sum_negative(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
         }
-        if (flip) {
+        if constexpr (sizeof(T) == 4 && RLIC_F32_FLIP_MUL) {
+            // one select and a packed multiply by -1 or 1 (exact, signed
+            // zeros and infinities included) instead of two selects
+            const float m = flip ? -1.f : 1.f;
+            const float2 f2 = mul2_rn(make_float2(pu, pv), make_float2(m, m));
+            pu = f2.x;
+            pv = f2.y;
+        } else if (flip) {
             pu = neg_(pu);
             pv = neg_(pv);
         }
