@@ -160,20 +160,18 @@ __device__ __forceinline__ T accumulate(T w, T x, T acc) {
 #ifndef RLIC_STILL_BRANCH_F32
 #define RLIC_STILL_BRANCH_F32 1
 #endif
-#ifndef RLIC_F32_FLIP_MUL
-#define RLIC_F32_FLIP_MUL 0
-#endif
-#ifndef RLIC_F32_STILL_SUM
-#define RLIC_F32_STILL_SUM 0
-#endif
+
 
 // Which operands of the time divisions are routed around the division
-// sequence (see abs_quotient): 0 none, 1 zero numerators, 2 zero numerators
-// and zero denominators.  1 is the fastest on the at-scale workload (8192^2
-// float32): zero numerators are frequent (reversals), zero components rare,
-// and the full guard's extra selects cost more than the slow paths it saves.
+// sequence (see abs_quotient): 0 none; 1 zero numerators, with selects of
+// the fixed results; 2 zero numerators and zero denominators; 3 zero
+// numerators, with the result from a multiply by zero.  3 is the fastest on
+// the at-scale workload (8192^2 float32; 1.6% ahead of 1 on the traced pass,
+// whose ALU pipe the selects load): zero numerators are frequent
+// (reversals), zero components rare, and the full guard's extra selects
+// cost more than the slow paths it saves.
 #ifndef RLIC_QUOTIENT_GUARD
-#define RLIC_QUOTIENT_GUARD 1
+#define RLIC_QUOTIENT_GUARD 3
 #endif
 
 // |a / b| rounded to nearest, for b not NaN.  A zero numerator or a zero
@@ -479,14 +477,7 @@ __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
 template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
                                             int& last, const Geometry<I>& g) {
-    bool still;
-    if constexpr (sizeof(T) == 4 && RLIC_F32_STILL_SUM) {
-        // |u| + |v| is zero exactly when both are (u, v are not NaN here, and
-        // a sum of two subnormals does not underflow to zero)
-        still = add_rn(abs_(u), abs_(v)) == T(0);
-    } else {
-        still = is_zero(u) & is_zero(v);
-    }
+    const bool still = is_zero(u) & is_zero(v);
     if constexpr (sizeof(T) == 4 && RLIC_STILL_BRANCH_F32) {
         if (still) return 0u;  // the state stays as it is (src/lib.rs:242-244)
     }
@@ -620,14 +611,7 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
         } else {
             flip = sum_negative(mul_rn(pu, st.lu), mul_rn(pv, st.lv));
         }
-        if constexpr (sizeof(T) == 4 && RLIC_F32_FLIP_MUL) {
-            // one select and a packed multiply by -1 or 1 (exact, signed
-            // zeros and infinities included) instead of two selects
-            const float m = flip ? -1.f : 1.f;
-            const float2 f2 = mul2_rn(make_float2(pu, pv), make_float2(m, m));
-            pu = f2.x;
-            pv = f2.y;
-        } else if (flip) {
+        if (flip) {
             pu = neg_(pu);
             pv = neg_(pv);
         }
