@@ -358,6 +358,12 @@ __device__ __forceinline__ float truncate_to_f32(double x) {
 // refused as well.  Every intermediate stays normal: |b| and |a| in
 // [2^-60, 2^61), quotients in (2^-121, 2^121), and a nonzero r is a
 // multiple of 2^-285.
+// 1: the reciprocal seed's Newton step runs on the FP32 pipe
+// (reciprocal_seed); 0: it runs as two FP64 FMAs.
+#ifndef RLIC_F64_SEED_FP32
+#define RLIC_F64_SEED_FP32 1
+#endif
+
 __device__ __forceinline__ double f32_to_f64_bits(float x) {
     // exact widening of a normal positive float32 with integer instructions
     const uint32_t b = __float_as_uint(x);
@@ -369,12 +375,52 @@ __device__ __forceinline__ float mantissa_f32(double x) {
     const uint64_t b = bits_of(x);
     return __uint_as_float((127u << 23) | uint32_t((b >> 29) & 0x7FFFFFu));
 }
+// The Newton step y1 = y0 + y0 (1 - B y0) on the FP32 pipe: B is split into
+// its leading 24 bits bh and the next 24 bits bm, the product bh y0 is
+// taken exactly (its rounding error by an FMA), and the correction
+// y0 (1 - (bh + bm) y0), about 2^-21 y0, is accurate to about 2^-45 y0.  y1
+// is assembled as a float64 from y0 and the correction with 64-bit integer
+// arithmetic (truncated to 53 bits).  Its accuracy, about 2^-42, only
+// affects how often the certificate of quotient_screened accepts, never
+// the correctness of an accepted quotient.
+__device__ __forceinline__ double reciprocal_seed(double B) {
+    const uint64_t bb = bits_of(B);
+    const uint32_t eb = uint32_t(bb >> 52) & 0x7FFu;  // biased exponent of B
+    const float bh = truncate_to_f32(B);
+    // bits 28..0 of the significand, value lo29 * 2^(eb - 1075), as a float
+    const uint32_t lo29 = uint32_t(bb) & 0x1FFFFFFFu;
+    const float lo_f = __uint2float_rz(lo29);  // exact leading 24 bits
+    const float bm = lo29 ? __uint_as_float(__float_as_uint(lo_f) - ((1075u - eb) << 23)) : 0.f;
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(bh));
+    const float hi = __fmul_rn(bh, r0);
+    const float lo = __fmaf_rn(bh, r0, -hi);  // exact: bh r0 = hi + lo
+    const float e = __fmaf_rn(-bm, r0, __fsub_rn(__fsub_rn(1.f, hi), lo));
+    const float c = __fmul_rn(r0, e);
+    // y1 = r0 + c: significands as 64-bit fixed point, r0's leading bit at 61
+    const uint32_t rb = __float_as_uint(r0), cb = __float_as_uint(c);
+    const int kr = int((rb >> 23) & 0xFFu), kc = int((cb >> 23) & 0xFFu);
+    int64_t y = int64_t((rb & 0x7FFFFFu) | 0x800000u) << 38;
+    const int d = kr - kc;
+    if ((cb & 0x7FFFFFFFu) != 0u && d >= 0 && d <= 61) {
+        const int64_t cs = (int64_t((cb & 0x7FFFFFu) | 0x800000u) << 38) >> d;
+        y = (cb >> 31) ? y - cs : y + cs;
+    }
+    const int msb = 63 - __clzll(y);  // 60, 61 or 62
+    const uint64_t mant = (uint64_t(y) >> (msb - 52)) & 0xFFFFFFFFFFFFFull;
+    return from_bits((uint64_t(msb + kr + 835) << 52) | mant);
+}
+
 __device__ __forceinline__ bool quotient_screened(double a, double b, double& q) {
     const double A = abs_(a), B = abs_(b);
+#if RLIC_F64_SEED_FP32
+    const double y1 = reciprocal_seed(B);
+#else
     float r0;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(truncate_to_f32(B)));
     const double y0 = f32_to_f64_bits(r0);
     const double y1 = fma_rn(y0, fma_rn(-B, y0, 1.0), y0);
+#endif
     const double q0 = mul_rn(A, y1);
     const double q1 = fma_rn(fma_rn(-B, q0, A), y1, q0);
     const double r = fma_rn(-B, q1, A);
