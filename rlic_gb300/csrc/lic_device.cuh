@@ -334,7 +334,7 @@ __device__ __forceinline__ float truncate_to_f32(double x) {
     return __uint_as_float((e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
 }
 // |a| / |b| rounded to nearest for nonzero a and b whose binary exponents
-// lie in [-60, 60] (the screened range), with 6 FP64 instructions instead of
+// lie in [-60, 60] (the screened range), with 4 FP64 instructions instead of
 // a general division; returns false when it cannot certify the result (the
 // caller then divides with __ddiv_rn).  Methods: Newton-Raphson refinement
 // of a reciprocal from a float32 seed (Markstein, "Computation of elementary
@@ -345,7 +345,8 @@ __device__ __forceinline__ float truncate_to_f32(double x) {
 // certificate:
 //
 //   y0 = rcp.approx(float32(|b|))          relative error < 2^-21
-//   y1 = y0 + y0 (1 - |b| y0)               relative error ~2^-42
+//   y1 = y0 + y0 (1 - |b| y0)               relative error ~2^-42 (FP32
+//                                           pipe, reciprocal_seed)
 //   q0 = |a| y1;  q1 = q0 + y1 (|a| - |b| q0)
 //   r  = fma(-|b|, q1, |a|)
 //
@@ -358,6 +359,7 @@ __device__ __forceinline__ float truncate_to_f32(double x) {
 // refused as well.  Every intermediate stays normal: |b| and |a| in
 // [2^-60, 2^61), quotients in (2^-121, 2^121), and a nonzero r is a
 // multiple of 2^-285.
+
 // 1: the reciprocal seed's Newton step runs on the FP32 pipe
 // (reciprocal_seed); 0: it runs as two FP64 FMAs.
 #ifndef RLIC_F64_SEED_FP32
