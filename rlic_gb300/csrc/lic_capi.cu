@@ -405,7 +405,11 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
     unsigned char* ws = d + (direct ? 2 : 4) * a_img;
     T* d_kernel = reinterpret_cast<T*>(ws + wl.kernel);
     unsigned* d_flag = reinterpret_cast<unsigned*>(ws + wl.total);
-    bool prefaulted = false;
+    // page-locked output is mapped already: nothing to touch
+    cudaPointerAttributes out_attr{};
+    bool prefaulted = cudaPointerGetAttributes(&out_attr, out) == cudaSuccess &&
+                      out_attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();  // a pageable pointer is not an error to keep
     auto prefault = [&]() {
         if (!prefaulted) touch_pages(out, n * sizeof(T));
         prefaulted = true;

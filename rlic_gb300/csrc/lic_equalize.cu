@@ -257,7 +257,7 @@ __global__ void tile_maps_kernel(const int32_t* __restrict__ bins, int64_t ny, i
 template <typename T>
 __device__ __forceinline__ T tile_centre(int64_t a, int64_t t, int64_t n) {
     const int64_t r0 = a * t, r1 = (r0 + t < n) ? r0 + t : n;
-    return div_rn_(T(r0 + r1 - 1), T(2));
+    return mul_rn_(T(r0 + r1 - 1), T(0.5));  // exact: the halving of an integer
 }
 
 // (a0, a1, f) of position i against the tile centres of one axis.
@@ -292,24 +292,44 @@ __device__ __forceinline__ T lerp_rn(T u, T w, T f) {
     return add_rn_(u, mul_rn_(f, sub_rn_(w, u)));
 }
 
+// (a0, a1, f) of every row (blockIdx.y == 0) or column (== 1) of the image.
+template <typename T>
+__global__ void axis_tables_kernel(int64_t ny, int64_t nx, int64_t th, int64_t tw, int64_t nty,
+                                   int64_t ntx, int32_t* __restrict__ a0, int32_t* __restrict__ a1,
+                                   T* __restrict__ f) {
+    const bool cols = blockIdx.y == 1;
+    const int64_t n = cols ? nx : ny, t = cols ? tw : th, nt = cols ? ntx : nty;
+    const int64_t base = cols ? ny : 0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        int64_t lo, hi;
+        T w;
+        interp_axis<T>(i, t, n, nt, lo, hi, w);
+        a0[base + i] = int32_t(lo);
+        a1[base + i] = int32_t(hi);
+        f[base + i] = w;
+    }
+}
+
 template <typename T>
 __global__ void map_tiles_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins,
-                                 int64_t ny, int64_t nx, int64_t th, int64_t tw, int64_t nty,
-                                 int64_t ntx, int nbins, const T* __restrict__ maps,
+                                 int64_t ny, int64_t nx, int64_t ntx, int nbins,
+                                 const int32_t* __restrict__ a0, const int32_t* __restrict__ a1,
+                                 const T* __restrict__ f, const T* __restrict__ maps,
                                  T* __restrict__ out) {
-    const int64_t n = ny * nx;
-    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= nx) return;
+    const int64_t ca0 = a0[ny + j], ca1 = a1[ny + j];
+    const T fx = f[ny + j];
+    for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
+        const int64_t k = i * nx + j;
         const int32_t b = bins[k];
         if (b < 0) {
             out[k] = x[k];
             continue;
         }
-        const int64_t i = k / nx, j = k - i * nx;
-        int64_t ra0, ra1, ca0, ca1;
-        T fy, fx;
-        interp_axis<T>(i, th, ny, nty, ra0, ra1, fy);
-        interp_axis<T>(j, tw, nx, ntx, ca0, ca1, fx);
+        const int64_t ra0 = a0[i], ra1 = a1[i];
+        const T fy = f[i];
         const T m00 = maps[(ra0 * ntx + ca0) * nbins + b];
         const T m01 = maps[(ra0 * ntx + ca1) * nbins + b];
         const T m10 = maps[(ra1 * ntx + ca0) * nbins + b];
@@ -385,6 +405,7 @@ size_t equalize_scratch_bytes(int64_t ny, int64_t nx, int64_t nbins, int strateg
     if (strategy == RLIC_EQUALIZE_TILE_INTERPOLATION) {
         const int64_t ntiles = ((ny + th - 1) / th) * ((nx + tw - 1) / tw);
         total += up(size_t(ntiles) * size_t(nbins) * elem);
+        total += 2 * up(size_t(ny + nx) * sizeof(int32_t)) + up(size_t(ny + nx) * elem);
     }
     return total;
 }
@@ -429,8 +450,17 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
         }
         kfn<<<unsigned(nty * ntx), 1024, smem, stream>>>(bins, ny, nx, th, tw, ntx, nbins, maps);
         count_launch();
-        map_tiles_kernel<T><<<grid_for(n), 256, 0, stream>>>(x, bins, ny, nx, th, tw, nty, ntx,
-                                                            nbins, maps, out);
+        unsigned char* tab = rest + up(size_t(nty * ntx) * size_t(nbins) * sizeof(T));
+        int32_t* a0 = reinterpret_cast<int32_t*>(tab);
+        int32_t* a1 = reinterpret_cast<int32_t*>(tab + up(size_t(ny + nx) * sizeof(int32_t)));
+        T* f = reinterpret_cast<T*>(tab + 2 * up(size_t(ny + nx) * sizeof(int32_t)));
+        const int64_t longest = ny > nx ? ny : nx;
+        axis_tables_kernel<T><<<dim3(unsigned((longest + 255) / 256), 2), 256, 0, stream>>>(
+            ny, nx, th, tw, nty, ntx, a0, a1, f);
+        count_launch();
+        const int64_t gy = ny < 1024 ? ny : 1024;
+        map_tiles_kernel<T><<<dim3(unsigned((nx + 255) / 256), unsigned(gy)), 256, 0, stream>>>(
+            x, bins, ny, nx, ntx, nbins, a0, a1, f, maps, out);
         count_launch();
     } else {
         const dim3 block(32, 8);
