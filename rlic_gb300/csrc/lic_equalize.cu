@@ -388,6 +388,54 @@ __device__ __forceinline__ void sliding_pixel(const T* __restrict__ x,
     out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
 }
 
+// Sliding tile with the bins of a CTA's 32 x 8 pixels and their windows
+// staged in shared memory (cells outside the image hold -1, which no count
+// includes).  Used when that region fits; the counts are the same as
+// sliding_pixel's.
+constexpr int kSlideBx = 32, kSlideBy = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kSlideBx * kSlideBy)
+sliding_smem_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins, int64_t ny,
+                    int64_t nx, int th, int tw, const Stats<T>* st, T* __restrict__ out) {
+    extern __shared__ int32_t s_bins[];
+    const int rw = kSlideBx + tw - 1, rh = kSlideBy + th - 1;  // region
+    const int64_t j0 = int64_t(blockIdx.x) * kSlideBx, i0 = int64_t(blockIdx.y) * kSlideBy;
+    const int64_t ri0 = i0 - th / 2, rj0 = j0 - tw / 2;
+    const int tid = threadIdx.y * kSlideBx + threadIdx.x;
+    for (int q = tid; q < rw * rh; q += kSlideBx * kSlideBy) {
+        const int qr = q / rw, qc = q - qr * rw;
+        const int64_t gi = ri0 + qr, gj = rj0 + qc;
+        s_bins[q] = (gi >= 0 && gi < ny && gj >= 0 && gj < nx) ? __ldg(bins + gi * nx + gj) : -1;
+    }
+    __syncthreads();
+    const int64_t i = i0 + threadIdx.y, j = j0 + threadIdx.x;
+    if (i >= ny || j >= nx) return;
+    const int64_t k = i * nx + j;
+    const int32_t b = s_bins[(threadIdx.y + th / 2) * rw + threadIdx.x + tw / 2];
+    if (b < 0) {
+        out[k] = x[k];
+        return;
+    }
+    const bool all_finite = st->count == (unsigned long long)(ny * nx);
+    const uint32_t ub = uint32_t(b);
+    uint32_t below = 0, valid = 0;
+    for (int r = 0; r < th; ++r) {
+        const int32_t* row = s_bins + (threadIdx.y + r) * rw + threadIdx.x;
+        for (int c = 0; c < tw; ++c) below += uint32_t(row[c]) <= ub;
+        if (!all_finite)
+            for (int c = 0; c < tw; ++c) valid += row[c] >= 0;
+    }
+    if (all_finite) {  // the window clipped to the image
+        const int64_t r0 = i - th / 2 < 0 ? 0 : i - th / 2;
+        const int64_t r1 = i - th / 2 + th > ny ? ny : i - th / 2 + th;
+        const int64_t c0 = j - tw / 2 < 0 ? 0 : j - tw / 2;
+        const int64_t c1 = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
+        valid = uint32_t((r1 - r0) * (c1 - c0));
+    }
+    out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
+}
+
 unsigned grid_for(int64_t n) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 8) blocks = 152 * 8;
@@ -463,10 +511,23 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
             x, bins, ny, nx, ntx, nbins, a0, a1, f, maps, out);
         count_launch();
     } else {
-        const dim3 block(32, 8);
         const int64_t gy = (ny + 7) / 8;
-        const dim3 grid(unsigned((nx + 31) / 32), unsigned(gy < 65535 ? gy : 65535));
-        sliding_kernel<T><<<grid, block, 0, stream>>>(x, bins, ny, nx, th, tw, st, out);
+        const size_t smem = size_t(kSlideBx + tw - 1) * size_t(kSlideBy + th - 1) * 4;
+        if (smem <= 200 * 1024 && gy <= 65535) {
+            auto kfn = sliding_smem_kernel<T>;
+            if (smem > 48 * 1024) {
+                e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem));
+                if (e != cudaSuccess) return e;
+            }
+            kfn<<<dim3(unsigned((nx + kSlideBx - 1) / kSlideBx), unsigned(gy)),
+                  dim3(kSlideBx, kSlideBy), smem, stream>>>(x, bins, ny, nx, int(th), int(tw),
+                                                            st, out);
+        } else {
+            const dim3 block(32, 8);
+            const dim3 grid(unsigned((nx + 31) / 32), unsigned(gy < 65535 ? gy : 65535));
+            sliding_kernel<T><<<grid, block, 0, stream>>>(x, bins, ny, nx, th, tw, st, out);
+        }
         count_launch();
     }
     return cudaGetLastError();
