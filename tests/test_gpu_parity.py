@@ -325,6 +325,36 @@ def test_fourier_vortex_full_size_properties(oracle) -> None:
     assert torch.equal(five.view(torch.int32), chain.view(torch.int32))
 
 
+def test_images_beyond_2_31_pixels() -> None:
+    """32768 x 65600 float32 (2.15e9 pixels): the 64-bit index kernels, traced
+    and replayed.  With u = 1 and v = 0 every streamline runs along its row
+    one cell per step (x periodic), so each pass is a row convolution whose
+    float32 result numpy reproduces exactly: the weights are powers of two,
+    so every product is exact and each sum rounds once, as the FMAs do."""
+    import torch
+
+    ny, nx = 32768, 65600
+    assert ny * nx > 2**31
+    gen = torch.Generator(device="cuda").manual_seed(8)
+    tex = torch.rand((ny, nx), generator=gen, device="cuda", dtype=torch.float32)
+    u = torch.ones_like(tex)
+    v = torch.zeros_like(tex)
+    k = torch.tensor([0.25, 0.5, 0.25], device="cuda", dtype=torch.float32)
+    out = rlic_gb300.convolve(tex, u, v, kernel=k, boundaries={"x": "periodic", "y": "closed"},
+                              iterations=2)
+    del u, v
+    f32 = np.float32
+
+    def row_pass(t):  # acc = 0.5 t[j]; acc += 0.25 t[j+1]; acc += 0.25 t[j-1]
+        acc = (f32(0.5) * t).astype(f32)
+        acc = (acc + f32(0.25) * np.roll(t, -1)).astype(f32)
+        return (acc + f32(0.25) * np.roll(t, 1)).astype(f32)
+
+    for i in (0, 1, 12345, ny - 2, ny - 1):
+        row = tex[i].cpu().numpy()
+        assert_bitwise(out[i].cpu().numpy(), row_pass(row_pass(row)))
+
+
 # ------------------------------------------------- public API / torch --
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
