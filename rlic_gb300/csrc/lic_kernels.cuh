@@ -348,9 +348,21 @@ lic_scatter_kernel(const T* __restrict__ g, const uint32_t* __restrict__ codes,
     }
 }
 
+// Sum of v over the warp, added by lane 0 to *addr (shared memory).  Every
+// lane of the warp must call it.
+template <typename T>
+__device__ __forceinline__ void warp_add_to(T* addr, T v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(addr, v);
+}
+
 // dw[k] += sum_p g[p] * x[c_k(p)]: the gradient of <g, A x> with respect to
-// kernel[k].  Per-CTA partial sums in shared memory, one global (float64)
-// atomic per tap per CTA.
+// kernel[k].  The lanes of a warp walk their pixels' taps in step, so every
+// tap's 32 products are summed across the warp with shuffles and added to
+// the CTA's shared partial sum by one lane (32 lanes adding to one shared
+// address would serialise); one global (float64) atomic per tap per CTA.
+// A lane past the image or past a stop code contributes zero.
 template <typename T, typename I>
 __global__ void __launch_bounds__(256)
 lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
@@ -362,12 +374,33 @@ lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
     for (int k = threadIdx.x; k < klen; k += blockDim.x) acc[k] = T(0);
     if (threadIdx.x == 0) fill_delta_table(table, geo.nx, geo.ny);
     __syncthreads();
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int lane = threadIdx.x & 31;
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < cl.npix; q += stride) {
-        const I p = I(q);
-        const T gp = g[p];
-        for_each_tap(p, codes, cl, klen, table,
-                     [&](int k, I cell) { atomicAdd(acc + k, mul_rn(gp, __ldg(x + cell))); });
+    // the loop bound is the warp's first pixel, so the whole warp iterates
+    for (int64_t q0 = int64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31); q0 < cl.npix;
+         q0 += stride) {
+        const int64_t q = q0 + lane;
+        const bool active = q < cl.npix;
+        const I p = active ? I(q) : I(0);
+        const T gp = active ? g[p] : T(0);
+        warp_add_to(acc + kmid, active ? mul_rn(gp, __ldg(x + p)) : T(0));
+        for (int half = 0; half < 2; ++half) {
+            const uint32_t* words =
+                codes + (half ? size_t(cl.words_f) * size_t(cl.npix) : size_t(0)) + p;
+            const int count = half ? kmid : nf;
+            I cell = p;
+            bool stopped = !active;
+            for (int s = 0; s < count; ++s) {
+                const uint32_t wd = __ldg(words + size_t(s >> 3) * size_t(cl.npix));
+                const uint32_t code = (wd >> (4 * (s & 7))) & 15u;
+                stopped = stopped || code == kStop;
+                if (!stopped) cell += table[code];
+                const T v = stopped ? T(0) : mul_rn(gp, __ldg(x + cell));
+                warp_add_to(acc + (half ? kmid - 1 - s : kmid + 1 + s), v);
+            }
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < klen; k += blockDim.x) atomicAdd(dw + k, double(acc[k]));
