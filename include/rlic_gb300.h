@@ -72,6 +72,7 @@ extern "C" {
 #define RLIC_FLAG_NO_BRANCHLESS 0x4u /* reference built without feature `branchless` */
 #define RLIC_FLAG_NO_PATH_CACHE 0x8u /* trace every streamline in every pass          */
 #define RLIC_FLAG_CHECK_TEXTURE 0x20u /* with HOST_MEMORY: fail if texture has x < 0   */
+#define RLIC_FLAG_FIELD_NAN_FREE 0x40u /* rlic_sweep_*: the packed field has no NaN   */
 
 /* Library version string. */
 RLIC_API const char *rlic_version(void);
@@ -84,7 +85,8 @@ RLIC_API const char *rlic_last_error(void);
  * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps,
  * `iterations` passes and the given flags: the packed (u, v) field, for two
  * or more iterations one ping-pong texture buffer and (unless
- * RLIC_FLAG_NO_PATH_CACHE) the path cache, and a copy of the kernel.
+ * RLIC_FLAG_NO_PATH_CACHE) the path cache, a copy of the kernel and a
+ * flag that records whether the field holds a NaN sample.
  * 0 on invalid arguments.
  */
 RLIC_API size_t rlic_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int64_t iterations,
@@ -340,7 +342,11 @@ RLIC_API int rlic_trace_cells_f64(const double *u, const double *v, int64_t ny, 
  * rlic_sweep_*: one convolution pass, `convolve` of src/lib.rs:364-406:
  *   tex_out = LIC(tex_in) along the packed field.  When `codes` is not NULL
  *   (rlic_path_code_bytes() bytes, 4-byte aligned) the pass also records
- *   every streamline step there.  `flags` takes the variant bits only.
+ *   every streamline step there.  `flags` takes the variant bits and
+ *   RLIC_FLAG_FIELD_NAN_FREE, a promise that the packed field holds no NaN
+ *   sample, which spares the steps their NaN test (the convolve entry points
+ *   find this out themselves while packing; with a NaN in the field the
+ *   results are then unspecified).
  *
  * rlic_replay_*: one convolution pass replayed from `codes` recorded by
  *   rlic_sweep_* on the same ny x nx image with the same klen (boundaries

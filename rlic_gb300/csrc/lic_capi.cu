@@ -162,6 +162,30 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 #define RLIC_HOST_CHUNKS 8
 #endif
 
+// A device word that stays zero: the "no NaN sample" flag of fields the
+// caller vouches for (RLIC_FLAG_FIELD_NAN_FREE).
+__device__ unsigned g_zero_flag = 0u;
+
+const unsigned* zero_flag(cudaError_t* err) {
+    static std::mutex mu;
+    static const unsigned* addr[64] = {};
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= 64) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        *err = cudaGetSymbolAddress(&p, g_zero_flag);
+        if (*err != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<const unsigned*>(p);
+    }
+    return addr[dev];
+}
+
 // A non-blocking stream per device for the uploads of host-memory calls, at
 // the greatest priority: the block scheduler then gives the upload kernels
 // the SM slots that the traced pass's blocks free, instead of queueing them
@@ -256,7 +280,7 @@ size_t code_bytes(int64_t ny, int64_t nx, int64_t klen) {
 }
 
 struct WorkspaceLayout {
-    size_t uv, tmp, codes, kernel, total;
+    size_t uv, tmp, codes, kernel, nan, total;
 };
 
 WorkspaceLayout workspace_layout(int64_t ny, int64_t nx, int64_t klen, int64_t iterations,
@@ -272,6 +296,8 @@ WorkspaceLayout workspace_layout(int64_t ny, int64_t nx, int64_t klen, int64_t i
     if (use_path_cache(iterations, klen, flags)) off += align_up(code_bytes(ny, nx, klen));
     w.kernel = off;
     off += align_up(size_t(klen) * s);
+    w.nan = off;  // flag: the packed field holds a NaN sample
+    off += align_up(sizeof(unsigned));
     w.total = off;
     return w;
 }
@@ -302,8 +328,13 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
     const bool cache = use_path_cache(iterations, klen, flags);
     const Shape sh = make_shape(ny, nx, bnd);
-    const LaunchConfig lc = launch_config();
-    if (!uv_ready) RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream));
+    LaunchConfig lc = launch_config();
+    if (!uv_ready) {
+        unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
+        RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
+        RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream, nan_flag));
+        lc.field_nan = nan_flag;
+    }
     const T* src = texture;
     for (int64_t it = 0; it < iterations; ++it) {
         T* dst = ((iterations - 1 - it) % 2 == 0) ? out : tmp;
@@ -444,6 +475,9 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         for (int k = 0; k < nchunks; ++k) arrival[order[k]] = k;
         events.resize(nchunks + 1, nullptr);
         for (auto& ev : events) RLIC_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        // the packs OR into the field's NaN flag; the traced pass reads it
+        unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
+        RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
         // the scratch was allocated stream-ordered on `stream`
         RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
         RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
@@ -491,7 +525,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                                                               d_tex + off, r1 - r0, nx, aux));
                     RLIC_CUDA_TRY(rlic::launch_pack_strided(u + r0 * st[2], st[2], st[3],
                                                             v + r0 * st[4], st[4], st[5],
-                                                            uv_rows, r1 - r0, nx, aux));
+                                                            uv_rows, r1 - r0, nx, aux, nan_flag));
                 } else {
                     RLIC_CUDA_TRY(cudaMemcpyAsync(d_tex + off, texture + off, cnt * sizeof(T),
                                                   cudaMemcpyHostToDevice, aux));
@@ -499,7 +533,8 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                                                   cudaMemcpyHostToDevice, aux));
                     RLIC_CUDA_TRY(cudaMemcpyAsync(d_v + off, v + off, cnt * sizeof(T),
                                                   cudaMemcpyHostToDevice, aux));
-                    RLIC_CUDA_TRY(rlic::launch_pack(d_u + off, d_v + off, uv_rows, int64_t(cnt), aux));
+                    RLIC_CUDA_TRY(rlic::launch_pack(d_u + off, d_v + off, uv_rows, int64_t(cnt),
+                                                    aux, nan_flag));
                 }
             }
             RLIC_CUDA_TRY(cudaEventRecord(events[k], aux));
@@ -517,6 +552,9 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 LaunchConfig part = lc;
                 part.tile_begin = tr * tiles_x;
                 part.tile_count = (tr_end - tr) * tiles_x;
+                // a NaN in a chunk that has not arrived yet cannot be reached
+                // from these tile rows, so the flag's value now suffices
+                part.field_nan = nan_flag;
                 RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen), sh,
                                                 part, dst_of(0), codes, stream));
                 tr = tr_end;
@@ -647,21 +685,27 @@ int sweep_impl(const T* tex_in, const void* uv, int64_t ny, int64_t nx, const T*
                void* codes, void* stream_, unsigned flags) {
     g_last_error.clear();
     const int bnd[4] = {bxl, bxr, byl, byr};
-    int rc = check_common(ny, nx, klen, uv_mode, bnd, flags);
+    int rc = check_common(ny, nx, klen, uv_mode, bnd, flags & ~RLIC_FLAG_FIELD_NAN_FREE);
     if (rc) return rc;
-    if (flags & (RLIC_FLAG_HOST_MEMORY | RLIC_FLAG_NO_PATH_CACHE))
-        return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes the variant flags only");
+    if (flags & (RLIC_FLAG_HOST_MEMORY | RLIC_FLAG_NO_PATH_CACHE | RLIC_FLAG_CHECK_TEXTURE))
+        return fail(RLIC_ERR_INVALID_ARGUMENT,
+                    "this entry point takes the variant flags and RLIC_FLAG_FIELD_NAN_FREE only");
     if (!tex_in || !uv || !kernel || !tex_out)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
     if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
     const Variant var = make_variant(flags, uv_mode);
+    LaunchConfig lc = launch_config();
+    if (flags & RLIC_FLAG_FIELD_NAN_FREE) {
+        cudaError_t e = cudaSuccess;
+        lc.field_nan = zero_flag(&e);
+        if (!lc.field_nan) return cuda_fail(e, "cudaGetSymbolAddress");
+    }
     RLIC_CUDA_TRY(rlic::launch_pass(var,
                                     (codes != nullptr && klen > 1) ? rlic::kPassSampleRecord
                                                                    : rlic::kPassSample,
-                                    tex_in, uv, kernel, int(klen), make_shape(ny, nx, bnd),
-                                    launch_config(), tex_out,
-                                    static_cast<uint32_t*>(codes),
+                                    tex_in, uv, kernel, int(klen), make_shape(ny, nx, bnd), lc,
+                                    tex_out, static_cast<uint32_t*>(codes),
                                     static_cast<cudaStream_t>(stream_)));
     return RLIC_OK;
 }
@@ -706,8 +750,9 @@ LowpLayout lowp_layout(int64_t ny, int64_t nx, int64_t klen, size_t s) {
     off += align_up(2 * n);
     w.w32 = off;
     off += align_up(size_t(klen) * 4);
-    w.scal = off;  // float 1/sum(|kernel|) at +0, double undo factor at +8
-    off += align_up(16);
+    w.scal = off;  // float 1/sum(|kernel|) at +0, double undo factor at +8,
+                   // NaN flag of the packed field at +16
+    off += align_up(20);
     w.total = off;
     return w;
 }
@@ -756,10 +801,14 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
         float* inv_scale = reinterpret_cast<float*>(ws + wl.scal);
         double* undo = reinterpret_cast<double*>(ws + wl.scal + 8);
         void* bufs[2] = {ws + wl.buf_a, ws + wl.buf_b};
-        RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream));
+        unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.scal + 16);
+        RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
+        RLIC_CUDA_TRY(rlic::launch_pack(u, v, uv, n, stream, nan_flag));
+        LaunchConfig trace_lc = lc;
+        trace_lc.field_nan = nan_flag;
         RLIC_CUDA_TRY(rlic::launch_pass(make_variant(flags, uv_mode), rlic::kPassRecordOnly,
                                         static_cast<const T*>(nullptr), uv, kernel, int(klen), sh,
-                                        lc, static_cast<T*>(nullptr), codes, stream));
+                                        trace_lc, static_cast<T*>(nullptr), codes, stream));
         RLIC_CUDA_TRY(rlic::launch_lowp_prepare(kernel, int(klen), iterations, w32, inv_scale,
                                                 undo, stream));
         RLIC_CUDA_TRY(rlic::launch_to_storage(texture, bufs[0], storage, n, stream));

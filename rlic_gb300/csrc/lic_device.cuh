@@ -648,14 +648,15 @@ struct TraceState {
 // backward trace, advance, then accumulate weight * texture at the new cell.
 // `code` receives the step code.
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
-          bool SAMPLE, typename I>
+          bool SAMPLE, typename I, bool NAN_CHECK = true>
 __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
                                            const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
                                            const T* __restrict__ tex, uint32_t& code) {
     const auto p = __ldg(uv + st.cell);
     T pu = p.x, pv = p.y;
-    if (is_nan(pu) || is_nan(pv)) return false;
+    // (NAN_CHECK false: the caller knows the field holds no NaN sample)
+    if (NAN_CHECK && (is_nan(pu) || is_nan(pv))) return false;
     if constexpr (POL) {
         bool flip;
         if constexpr (sizeof(T) == 4) {
@@ -691,7 +692,7 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
 // RECORD the word is stored at words[group * stride].  A trace that stops on
 // NaN stores the stop code in place of its step and nothing after it.
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
-          bool SAMPLE, bool RECORD, typename I>
+          bool SAMPLE, bool RECORD, typename I, bool NAN_CHECK = true>
 __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
                                            const T* __restrict__ tex, const T* w, int count,
@@ -712,7 +713,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK>(
                     st, acc, SAMPLE ? wq[b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                 return;
@@ -726,7 +727,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
         uint32_t word = 0;
         for (int b = 0; b < rest; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK>(
                     st, acc, SAMPLE ? w[8 * full + b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(full) * stride] = word | (kStop << (4 * b));
                 return;

@@ -72,14 +72,18 @@ template <> struct PassMinBlocks<double, int32_t> {
 
 template <typename T>
 __global__ void pack_uv_kernel(const T* __restrict__ u, const T* __restrict__ v,
-                               typename Vec2<T>::type* __restrict__ uv, int64_t n) {
+                               typename Vec2<T>::type* __restrict__ uv, int64_t n,
+                               unsigned* __restrict__ nan_flag) {
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    bool nan = false;
     for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
         typename Vec2<T>::type p;
         p.x = u[k];
         p.y = v[k];
+        nan |= isnan(p.x) || isnan(p.y);
         uv[k] = p;
     }
+    if (nan && nan_flag) atomicOr(nan_flag, 1u);
 }
 
 // Tile bookkeeping shared by the pass and gather kernels.
@@ -127,7 +131,8 @@ struct CodeLayout {
 // (kRecordOnly, no texture read and no output).
 enum PassMode : int { kSample = 0, kSampleRecord = 1, kRecordOnly = 2 };
 
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, int MODE, typename I>
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, int MODE, typename I,
+          bool NAN_CHECK = true>
 __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
                                             const typename Vec2<T>::type* __restrict__ uv,
                                             const T* __restrict__ tex, const T* wf, const T* wb,
@@ -140,10 +145,10 @@ __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
     if constexpr (SAMPLE) acc = accumulate<T, FMA>(wmid, __ldg(tex + p), T(0));
     uint32_t* words_f = RECORD ? codes + p : nullptr;
     uint32_t* words_b = RECORD ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : nullptr;
-    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD>(acc, i, j, g, uv, tex, wf,
-                                                                     nf, words_f, cl.npix);
-    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD>(acc, i, j, g, uv, tex, wb,
-                                                                    kmid, words_b, cl.npix);
+    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD, I, NAN_CHECK>(
+        acc, i, j, g, uv, tex, wf, nf, words_f, cl.npix);
+    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD, I, NAN_CHECK>(
+        acc, i, j, g, uv, tex, wb, kmid, words_b, cl.npix);
     return acc;
 }
 
@@ -153,7 +158,8 @@ template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
 __global__ void __launch_bounds__(256, (PassMinBlocks<T, I>::value))
 lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __restrict__ uv,
                 const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
-                T* __restrict__ tex_out, uint32_t* __restrict__ codes, CodeLayout cl) {
+                T* __restrict__ tex_out, uint32_t* __restrict__ codes, CodeLayout cl,
+                const unsigned* __restrict__ field_nan) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* wsm = reinterpret_cast<T*>(smem_raw);
     const int kmid = klen / 2;
@@ -170,9 +176,17 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
     const I i = ti * tg.by + I(threadIdx.y);
     const I j = tj * tg.bx + I(threadIdx.x);
     T acc;
+    // a field known to hold no NaN sample spares interior tiles the per-step
+    // NaN test (and the stop-code exits of the recording loop)
+    const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
     if (tile_is_interior(ti, tj, tg, g)) {
-        acc = convolve_pixel<T, FMA, BRANCHLESS, POL, false, MODE>(
-            i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+        if (nan_free) {
+            acc = convolve_pixel<T, FMA, BRANCHLESS, POL, false, MODE, I, false>(
+                i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+        } else {
+            acc = convolve_pixel<T, FMA, BRANCHLESS, POL, false, MODE, I, true>(
+                i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
+        }
     } else if (i < g.ny && j < g.nx) {
         acc = convolve_pixel<T, FMA, BRANCHLESS, POL, true, MODE>(
             i, j, g, uv, tex_in, wsm, wsm + nf_pad, wmid, nf, kmid, codes, cl);
@@ -456,9 +470,10 @@ template <typename T>
 __global__ void pack_uv_strided_kernel(const T* __restrict__ u, int64_t su0, int64_t su1,
                                        const T* __restrict__ v, int64_t sv0, int64_t sv1,
                                        typename Vec2<T>::type* __restrict__ uv, int64_t ny,
-                                       int64_t nx) {
+                                       int64_t nx, unsigned* __restrict__ nan_flag) {
     constexpr int U = kUploadUnroll / 2;  // two loads per element
     const int64_t span = int64_t(blockDim.x) * U;
+    bool nan = false;
     for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
         for (int64_t j0 = int64_t(blockIdx.x) * span + threadIdx.x; j0 < nx;
              j0 += int64_t(gridDim.x) * span) {
@@ -474,10 +489,14 @@ __global__ void pack_uv_strided_kernel(const T* __restrict__ u, int64_t su0, int
 #pragma unroll
             for (int k = 0; k < U; ++k) {
                 const int64_t j = j0 + int64_t(k) * blockDim.x;
-                if (j < nx) uv[i * nx + j] = r[k];
+                if (j < nx) {
+                    nan |= isnan(r[k].x) || isnan(r[k].y);
+                    uv[i * nx + j] = r[k];
+                }
             }
         }
     }
+    if (nan && nan_flag) atomicOr(nan_flag, 1u);
 }
 
 // Contiguous rows with 16-byte aligned starts: plain 16-byte vector copies
@@ -505,11 +524,24 @@ __global__ void copy_vec16_kernel(const uint4* __restrict__ src, uint4* __restri
 // Contiguous u, v with 16-byte aligned rows: 16-byte vectors of u and of v
 // interleaved into two 16-byte vectors of (u, v) pairs.  ELEM_WORDS is the
 // element size in 32-bit words (1: float, 2: double).
+// A NaN has all exponent bits set and a nonzero fraction.
+__device__ __forceinline__ bool nan_in(uint4 w, int elem_words) {
+    if (elem_words == 1) {
+        return ((w.x & 0x7FFFFFFFu) > 0x7F800000u) || ((w.y & 0x7FFFFFFFu) > 0x7F800000u) ||
+               ((w.z & 0x7FFFFFFFu) > 0x7F800000u) || ((w.w & 0x7FFFFFFFu) > 0x7F800000u);
+    }
+    const uint64_t a = (uint64_t(w.y) << 32 | w.x) & 0x7FFFFFFFFFFFFFFFull;
+    const uint64_t b = (uint64_t(w.w) << 32 | w.z) & 0x7FFFFFFFFFFFFFFFull;
+    return a > 0x7FF0000000000000ull || b > 0x7FF0000000000000ull;
+}
+
 template <int ELEM_WORDS>
 __global__ void pack_vec16_kernel(const uint4* __restrict__ u, const uint4* __restrict__ v,
-                                  uint4* __restrict__ uv, int64_t nvec) {
+                                  uint4* __restrict__ uv, int64_t nvec,
+                                  unsigned* __restrict__ nan_flag) {
     constexpr int U = kUploadUnroll / 2;
     const int64_t span = int64_t(blockDim.x) * U;
+    bool nan = false;
     for (int64_t b = int64_t(blockIdx.x) * span + threadIdx.x; b < nvec;
          b += int64_t(gridDim.x) * span) {
         uint4 a[U], c[U];
@@ -525,6 +557,7 @@ __global__ void pack_vec16_kernel(const uint4* __restrict__ u, const uint4* __re
         for (int k = 0; k < U; ++k) {
             const int64_t q = b + int64_t(k) * blockDim.x;
             if (q < nvec) {
+                nan |= nan_in(a[k], ELEM_WORDS) || nan_in(c[k], ELEM_WORDS);
                 if constexpr (ELEM_WORDS == 1) {
                     uv[2 * q] = make_uint4(a[k].x, c[k].x, a[k].y, c[k].y);
                     uv[2 * q + 1] = make_uint4(a[k].z, c[k].z, a[k].w, c[k].w);
@@ -535,6 +568,7 @@ __global__ void pack_vec16_kernel(const uint4* __restrict__ u, const uint4* __re
             }
         }
     }
+    if (nan && nan_flag) atomicOr(nan_flag, 1u);
 }
 
 // Grid of an upload over ny rows of nx elements, `per_thread` elements per
@@ -690,12 +724,13 @@ cudaError_t persistent_grid(K kernel, int threads, size_t smem, int64_t ntiles,
 }
 
 template <typename T>
-cudaError_t launch_pack_t(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) {
+cudaError_t launch_pack_t(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream,
+                          unsigned* nan_flag) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
     pack_uv_kernel<T><<<unsigned(blocks), 256, 0, stream>>>(
-        u, v, static_cast<typename Vec2<T>::type*>(uv), n);
+        u, v, static_cast<typename Vec2<T>::type*>(uv), n, nan_flag);
     count_launch();
     return cudaGetLastError();
 }
@@ -719,7 +754,7 @@ cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int 
     if (count <= 0) return cudaSuccess;
     kfn<<<unsigned(count), dim3(lc.block_x, lc.block_y), smem, stream>>>(
         tex_in, static_cast<const typename Vec2<T>::type*>(uv), kernel, klen, g, tg, tex_out,
-        codes, cl);
+        codes, cl, lc.field_nan);
     count_launch();
     return cudaGetLastError();
 }
@@ -822,7 +857,7 @@ inline unsigned stream_blocks(int64_t n) {
 template <typename T>
 cudaError_t launch_pack_strided_t(const T* u, int64_t su0, int64_t su1, const T* v, int64_t sv0,
                                   int64_t sv1, void* uv, int64_t ny, int64_t nx,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, unsigned* nan_flag) {
     const int64_t per_vec = 16 / int64_t(sizeof(T));
     if (su1 == 1 && sv1 == 1 && su0 == nx && sv0 == nx && nx % per_vec == 0 && aligned16(u) &&
         aligned16(v) && aligned16(uv)) {
@@ -830,10 +865,10 @@ cudaError_t launch_pack_strided_t(const T* u, int64_t su0, int64_t su1, const T*
         const dim3 grid = upload_grid(1, nvec, kUploadUnroll / 2);
         pack_vec16_kernel<int(sizeof(T) / 4)><<<grid.x, 256, 0, stream>>>(
             reinterpret_cast<const uint4*>(u), reinterpret_cast<const uint4*>(v),
-            static_cast<uint4*>(uv), nvec);
+            static_cast<uint4*>(uv), nvec, nan_flag);
     } else {
         pack_uv_strided_kernel<T><<<upload_grid(ny, nx, kUploadUnroll / 2), 256, 0, stream>>>(
-            u, su0, su1, v, sv0, sv1, static_cast<typename Vec2<T>::type*>(uv), ny, nx);
+            u, su0, su1, v, sv0, sv1, static_cast<typename Vec2<T>::type*>(uv), ny, nx, nan_flag);
     }
     count_launch();
     return cudaGetLastError();
@@ -935,8 +970,9 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
 
 // Definitions of the per-type overloads declared in lic_launch.h.
 #define RLIC_DEFINE_LAUNCHERS(T)                                                             \
-    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream) { \
-        return launch_pack_t<T>(u, v, uv, n, stream);                                        \
+    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream, \
+                            unsigned* nan_flag) {                                            \
+        return launch_pack_t<T>(u, v, uv, n, stream, nan_flag);                              \
     }                                                                                        \
     cudaError_t launch_pass(const Variant& var, int mode, const T* tex_in, const void* uv,    \
                             const T* kernel, int klen, const Shape& sh,                      \
@@ -986,8 +1022,9 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
     }                                                                                        \
     cudaError_t launch_pack_strided(const T* u, int64_t su0, int64_t su1, const T* v,        \
                                     int64_t sv0, int64_t sv1, void* uv, int64_t ny,          \
-                                    int64_t nx, cudaStream_t stream) {                       \
-        return launch_pack_strided_t<T>(u, su0, su1, v, sv0, sv1, uv, ny, nx, stream);       \
+                                    int64_t nx, cudaStream_t stream, unsigned* nan_flag) {   \
+        return launch_pack_strided_t<T>(u, su0, su1, v, sv0, sv1, uv, ny, nx, stream,        \
+                                        nan_flag);                                           \
     }                                                                                        \
     cudaError_t launch_gather_strided(const T* src, int64_t s0, int64_t s1, T* dst,          \
                                       int64_t ny, int64_t nx, cudaStream_t stream) {         \

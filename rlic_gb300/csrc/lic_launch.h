@@ -33,6 +33,9 @@ struct LaunchConfig {
     // tile_count) of the row-major tile grid (tile_count 0: all tiles)
     int64_t tile_begin = 0;
     int64_t tile_count = 0;
+    // traced passes only: device flag that the pack kernels set when the
+    // field holds a NaN sample (null: unknown, so every step checks)
+    const unsigned* field_nan = nullptr;
 };
 
 // What a traced pass does per step: sample the texture, sample and record the
@@ -57,7 +60,8 @@ inline int64_t code_words_per_pixel(int64_t klen) {
 }
 
 #define RLIC_DECLARE_LAUNCHERS(T)                                                          \
-    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream); \
+    cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream, \
+                            unsigned* nan_flag = nullptr);                                 \
     cudaError_t launch_pass(const Variant& var, int mode, const T* tex_in, const void* uv,    \
                             const T* kernel, int klen, const Shape& sh,                    \
                             const LaunchConfig& lc, T* tex_out, uint32_t* codes,           \
@@ -79,7 +83,8 @@ inline int64_t code_words_per_pixel(int64_t klen) {
                                       cudaStream_t stream);                                \
     cudaError_t launch_pack_strided(const T* u, int64_t su0, int64_t su1, const T* v,      \
                                     int64_t sv0, int64_t sv1, void* uv, int64_t ny,        \
-                                    int64_t nx, cudaStream_t stream);                      \
+                                    int64_t nx, cudaStream_t stream,                       \
+                                    unsigned* nan_flag = nullptr);                         \
     cudaError_t launch_gather_strided(const T* src, int64_t s0, int64_t s1, T* dst,        \
                                       int64_t ny, int64_t nx, cudaStream_t stream);        \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel,         \

@@ -35,13 +35,13 @@ def test_version(native) -> None:
 def test_workspace_bytes(native) -> None:
     ws = native.rlic_workspace_bytes
     n = 8192 * 8192
-    # one pass: packed (u, v) + kernel copy
-    assert ws(8192, 8192, 65, 1, 4, 0) == 2 * n * 4 + 512
+    # one pass: packed (u, v) + kernel copy + the field's NaN flag
+    assert ws(8192, 8192, 65, 1, 4, 0) == 2 * n * 4 + 512 + 256
     # five passes: + ping-pong buffer + path cache (8 words of 8 steps per pixel)
-    assert ws(8192, 8192, 65, 5, 4, 0) == 3 * n * 4 + 8 * 4 * n + 512
-    assert ws(8192, 8192, 65, 5, 4, 0x8) == 3 * n * 4 + 512
-    assert ws(10, 10, 3, 2, 8, 0) == 1792 + 1024 + 1024 + 256
-    assert ws(10, 10, 3, 2, 8, 0x8) == 1792 + 1024 + 256
+    assert ws(8192, 8192, 65, 5, 4, 0) == 3 * n * 4 + 8 * 4 * n + 512 + 256
+    assert ws(8192, 8192, 65, 5, 4, 0x8) == 3 * n * 4 + 512 + 256
+    assert ws(10, 10, 3, 2, 8, 0) == 1792 + 1024 + 1024 + 256 + 256
+    assert ws(10, 10, 3, 2, 8, 0x8) == 1792 + 1024 + 256 + 256
     assert ws(0, 10, 3, 1, 4, 0) == 0
     assert ws(10, 10, 3, 1, 2, 0) == 0
 

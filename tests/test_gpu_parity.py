@@ -176,6 +176,28 @@ def test_random_fields(oracle, dtype, uv_mode, bnd, kind) -> None:
     )
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("where", ["none", "centre", "corner"])
+def test_nan_free_fields_and_isolated_nans(oracle, dtype, where) -> None:
+    """Interior tiles of a field without NaN samples skip the per-step NaN
+    test; one NaN sample anywhere sends every step back to the checked path.
+    Both must give the oracle's bits and cells."""
+    rng = np.random.default_rng(21)
+    ny, nx = 96, 160
+    u, v = _field(rng, ny, nx, dtype, "random")
+    if where == "centre":
+        u[48, 80] = np.nan
+    elif where == "corner":
+        v[0, 0] = np.nan
+    tex = rng.random((ny, nx)).astype(dtype)
+    k = np.hanning(17).astype(dtype)
+    for mode in ("velocity", "polarization"):
+        want = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries="periodic", iterations=3)
+        assert_bitwise(capi_convolve(tex, u, v, k, mode, "periodic", iterations=3), want)
+        assert_bitwise(capi_convolve(tex, u, v, k, mode, "periodic", iterations=3,
+                                     extra_flags=_native.RLIC_FLAG_NO_PATH_CACHE), want)
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("uv_mode", ["velocity", "polarization"])
 def test_float64_near_ties_and_exponent_edges(oracle, variant, uv_mode) -> None:
@@ -448,6 +470,47 @@ def test_device_entry_points_with_workspace(oracle) -> None:
     assert_bitwise(out.cpu().numpy(), want2)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sweep_with_a_nan_free_promise(oracle, dtype) -> None:
+    """RLIC_FLAG_FIELD_NAN_FREE on a field without NaN samples gives the same
+    bits and codes as the checked steps."""
+    import torch
+
+    lib = _native.lib()
+    sfx = "f32" if dtype == np.float32 else "f64"
+    rng = np.random.default_rng(23)
+    ny, nx, klen = 120, 200, 21
+    u, v = _field(rng, ny, nx, dtype, "random")
+    tex = rng.random((ny, nx)).astype(dtype)
+    k = np.hanning(klen).astype(dtype)
+    d = {n: torch.from_numpy(a).cuda() for n, a in dict(t=tex, u=u, v=v, k=k).items()}
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    uv = torch.empty((ny, nx, 2), dtype=d["t"].dtype, device="cuda")
+    _native.check(getattr(lib, f"rlic_pack_field_{sfx}")(d["u"].data_ptr(), d["v"].data_ptr(),
+                                                         ny, nx, uv.data_ptr(), stream))
+    outs, codes = [], []
+    for flags in (0, _native.RLIC_FLAG_FIELD_NAN_FREE):
+        out = torch.empty_like(d["t"])
+        c = torch.empty(lib.rlic_path_code_bytes(ny, nx, klen) // 4, dtype=torch.int32,
+                        device="cuda")
+        _native.check(getattr(lib, f"rlic_sweep_{sfx}")(
+            d["t"].data_ptr(), uv.data_ptr(), ny, nx, d["k"].data_ptr(), klen, 1, 1, 1, 0, 0,
+            out.data_ptr(), c.data_ptr(), stream, flags))
+        outs.append(out.cpu().numpy())
+        codes.append(c.cpu().numpy())
+    want = oracle.convolve(tex, u, v, k, uv_mode="polarization",
+                           boundaries={"x": "periodic", "y": "closed"})
+    assert_bitwise(outs[0], want)
+    assert_bitwise(outs[1], want)
+    np.testing.assert_array_equal(codes[0], codes[1])
+    # the convolve entry points take no such promise: they find it out
+    rc = getattr(lib, f"rlic_convolve_{sfx}")(
+        d["t"].data_ptr(), d["u"].data_ptr(), d["v"].data_ptr(), ny, nx, d["k"].data_ptr(),
+        klen, 1, 1, 1, 0, 0, 1, torch.empty_like(d["t"]).data_ptr(), None, 0, stream,
+        _native.RLIC_FLAG_FIELD_NAN_FREE)
+    assert rc == _native.RLIC_ERR_INVALID_ARGUMENT
+
+
 def test_host_path_checks_negative_texture_on_device() -> None:
     rng = np.random.default_rng(31)
     tex = rng.random((64, 80))
@@ -513,12 +576,17 @@ def test_host_path_row_chunks(bnd, klen, iterations) -> None:
     """Host arrays of 4 Mpx and more go up in row chunks, with the traced pass
     started per group of tile rows as their rows and halo arrive (across the
     seam for a periodic y axis): same bits as the device-resident path,
-    contiguous and strided, on a ragged row count."""
+    contiguous and strided, on a ragged row count, with and without NaN
+    samples in the last chunk."""
     import torch
 
     rng = np.random.default_rng(klen)
     ny, nx = 2101, 2050
-    u, v = _field(rng, ny, nx, np.float32, "specials")
+    u, v = _field(rng, ny, nx, np.float32, "random")
+    if klen != 33:
+        # NaN samples only in the last rows: tile rows traced before that
+        # chunk arrives take the NaN-free steps, the others check every step
+        u[ny - 40:ny - 30, 100:140] = np.nan
     tex = rng.random((ny, nx), dtype=np.float32)
     k = np.hanning(klen).astype(np.float32)
     kw = dict(uv_mode="polarization", boundaries=bnd, iterations=iterations)
