@@ -89,26 +89,31 @@ batch_pass_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv) {
     const bool record = b.iterations >= 2;
     const bool interior = tile_is_interior(ti, tj, tg, g);
     if (!interior && (i >= b.ny || j >= b.nx)) return;
+    // interior tiles of a field without NaN samples skip the per-step NaN test
+    const bool fast = interior && __ldg(b.nan_flag) == 0u;
     float acc;
-#define RLIC_BATCH_PIXEL(POL, EDGE, MODE)                                                 \
-    acc = convolve_pixel<float, true, true, POL, EDGE, MODE>(i, j, g, uv, src, wsm,        \
-                                                            wsm + nf_pad, wmid, nf, kmid, \
-                                                            b.codes, cl)
+#define RLIC_BATCH_PIXEL(POL, EDGE, MODE, CHECK)                                           \
+    acc = convolve_pixel<float, true, true, POL, EDGE, MODE, int32_t, CHECK>(               \
+        i, j, g, uv, src, wsm, wsm + nf_pad, wmid, nf, kmid, b.codes, cl)
     if (b.pol) {
         if (record) {
-            if (interior) RLIC_BATCH_PIXEL(true, false, kSampleRecord);
-            else RLIC_BATCH_PIXEL(true, true, kSampleRecord);
+            if (fast) RLIC_BATCH_PIXEL(true, false, kSampleRecord, false);
+            else if (interior) RLIC_BATCH_PIXEL(true, false, kSampleRecord, true);
+            else RLIC_BATCH_PIXEL(true, true, kSampleRecord, true);
         } else {
-            if (interior) RLIC_BATCH_PIXEL(true, false, kSample);
-            else RLIC_BATCH_PIXEL(true, true, kSample);
+            if (fast) RLIC_BATCH_PIXEL(true, false, kSample, false);
+            else if (interior) RLIC_BATCH_PIXEL(true, false, kSample, true);
+            else RLIC_BATCH_PIXEL(true, true, kSample, true);
         }
     } else {
         if (record) {
-            if (interior) RLIC_BATCH_PIXEL(false, false, kSampleRecord);
-            else RLIC_BATCH_PIXEL(false, true, kSampleRecord);
+            if (fast) RLIC_BATCH_PIXEL(false, false, kSampleRecord, false);
+            else if (interior) RLIC_BATCH_PIXEL(false, false, kSampleRecord, true);
+            else RLIC_BATCH_PIXEL(false, true, kSampleRecord, true);
         } else {
-            if (interior) RLIC_BATCH_PIXEL(false, false, kSample);
-            else RLIC_BATCH_PIXEL(false, true, kSample);
+            if (fast) RLIC_BATCH_PIXEL(false, false, kSample, false);
+            else if (interior) RLIC_BATCH_PIXEL(false, false, kSample, true);
+            else RLIC_BATCH_PIXEL(false, true, kSample, true);
         }
     }
 #undef RLIC_BATCH_PIXEL
@@ -155,8 +160,13 @@ __global__ void batch_pack_kernel(const BatchInstance* __restrict__ insts) {
     const int64_t n = int64_t(b.ny) * b.nx;
     float2* uv = static_cast<float2*>(b.uv);
     const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride)
-        uv[k] = make_float2(b.u[k], b.v[k]);
+    bool nan = false;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const float2 p = make_float2(b.u[k], b.v[k]);
+        nan |= isnan(p.x) || isnan(p.y);
+        uv[k] = p;
+    }
+    if (nan) atomicOr(b.nan_flag, 1u);
 }
 
 }  // namespace

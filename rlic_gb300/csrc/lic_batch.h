@@ -23,6 +23,7 @@ struct BatchInstance {
     float* tmp;
     void* uv;
     uint32_t* codes;
+    unsigned* nan_flag;  // set by the pack when the field holds a NaN sample
     int ny, nx, klen, iterations, pol;
     int bnd[4];
     int tile_x, tile_y, tiles_x, ntiles;

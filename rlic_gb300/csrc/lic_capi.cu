@@ -870,7 +870,7 @@ int kernel_grad_impl(const T* g, const T* x, const void* codes, int64_t ny, int6
 // ------------------------------------------------------------ batched form --
 
 struct BatchLayout {
-    size_t insts, levels, total;
+    size_t insts, levels, flags, total;
     std::vector<size_t> uv, tmp, codes;  // per item
     int max_iterations;
 };
@@ -908,6 +908,8 @@ BatchLayout batch_layout(const rlic_batch_item_f32* items, int count) {
     for (int k = 0; k < count; ++k) L.max_iterations = std::max<int>(L.max_iterations, int(items[k].iterations));
     L.levels = off;
     off += align_up(size_t(std::max(L.max_iterations, 1)) * size_t(count) * (sizeof(int64_t) + sizeof(int)));
+    L.flags = off;  // one NaN flag per item
+    off += align_up(size_t(count) * sizeof(unsigned));
     for (int k = 0; k < count; ++k) {
         const auto& it = items[k];
         const size_t n = size_t(it.ny) * size_t(it.nx);
@@ -958,6 +960,7 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
         b.tmp = reinterpret_cast<float*>(ws + L.tmp[k]);
         b.uv = ws + L.uv[k];
         b.codes = reinterpret_cast<uint32_t*>(ws + L.codes[k]);
+        b.nan_flag = reinterpret_cast<unsigned*>(ws + L.flags) + k;
         b.ny = int(it.ny);
         b.nx = int(it.nx);
         b.klen = int(it.klen);
@@ -1001,6 +1004,7 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
             RLIC_CUDA_TRY(cudaMemsetAsync(items[k].out, 0,
                                           size_t(items[k].ny) * size_t(items[k].nx) * 4, stream));
     if (L.max_iterations == 0) return RLIC_OK;
+    RLIC_CUDA_TRY(cudaMemsetAsync(ws + L.flags, 0, size_t(count) * sizeof(unsigned), stream));
     RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
     for (int level = 1; level <= L.max_iterations; ++level)
         RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));
