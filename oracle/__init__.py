@@ -2,6 +2,6 @@
 equalization (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use this package, as the checker; the product package
-``rlic_gb300`` never imports it.
+``bench.py`` use this package, to check or time the CUDA path; the product
+package ``rlic_gb300`` never imports it.
 """

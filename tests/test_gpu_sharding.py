@@ -1,6 +1,6 @@
-"""Row-band sharding with the GPU pass: two ranks (processes) on the one GPU
-of the box, exchanging halo rows over a `gloo` group between passes, give
-the full image's bits.
+"""Row-band sharding with the GPU pass: two ranks (processes) on one GPU,
+exchanging halo rows over a `gloo` group between passes, give the full
+image's bits.
 
 The ranks' kernels never wait on each other: every exchange happens on the
 host between passes.
