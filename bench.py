@@ -489,7 +489,9 @@ def run_gb300(args, dist: Dist) -> None:
                 "plain": {"value": plain_value, "ms_per_step": plain_ms},
             },
         }
-        if not args.no_cpu_baseline:
+        # the CPU baseline is a single-GPU figure: at N > 1 the host cores
+        # are shared with the other ranks' processes, so it is left out
+        if not args.no_cpu_baseline and dist.world == 1:
             from oracle import oracle
 
             case_np = {x: case[x].cpu().numpy() for x in ("texture", "u", "v", "kernel")}
