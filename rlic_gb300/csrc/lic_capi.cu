@@ -1067,7 +1067,8 @@ int convolve_noalloc_f32(const float* texture, const float* u, const float* v, i
     if (rc) return rc;
     // Every region of the scratch is written before it is read (packed field,
     // ping-pong buffer, path codes), so the previous call's contents need no
-    // clearing.
+    // clearing; the one word that must start at zero, the field's NaN flag,
+    // is zeroed by run_device on the stream before the pack kernel sets it.
     return run_device<float>(texture, u, v, ny, nx, kernel, klen, make_variant(flags, uv_mode),
                              bnd, iterations, out, ws, flags, static_cast<cudaStream_t>(stream_));
 }
