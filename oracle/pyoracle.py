@@ -4,8 +4,11 @@ TEST INFRASTRUCTURE ONLY.  A second, independent restatement of the
 reference's native core (neutrinoceros/rlic src/lib.rs:157-443) used to
 cross-check the C oracle (lic_oracle.c) on small cases: scalar numpy
 arithmetic in the input dtype, with ``mul_add`` evaluated exactly on
-rationals and rounded once (Python 3.12 has no math.fma).  Default build
-only (features ``fma`` + ``branchless``).
+rationals and rounded once (Python 3.12 has no math.fma).  ``variant``
+selects the reference's Cargo feature set as the C oracle does: bit 0 =
+``fma`` (``mul_add`` fused; otherwise a rounded product, then a rounded
+sum), bit 1 = ``branchless`` (src/lib.rs:157-180); 3, both on, is the
+reference's default build.
 """
 
 from __future__ import annotations
@@ -14,6 +17,10 @@ import math
 from fractions import Fraction
 
 import numpy as np
+
+VARIANT_FMA = 1
+VARIANT_BRANCHLESS = 2
+DEFAULT_VARIANT = VARIANT_FMA | VARIANT_BRANCHLESS
 
 
 def _round_fraction(x: Fraction, dtype) -> float:
@@ -66,32 +73,47 @@ def signum(x, dtype):
     return dtype(-1.0) if np.signbit(x) else dtype(1.0)
 
 
-def time_to_next_pixel(vel, frac, dtype):
-    """src/lib.rs:168-179 (branchless + fma)."""
+def mul_add(a, b, c, dtype, variant=DEFAULT_VARIANT):
+    """``a.mul_add(b, c)`` with the ``fma`` feature, ``c += a * b`` without it
+    (src/lib.rs:174-177, 226-232, 353-360, 376-383)."""
+    if variant & VARIANT_FMA:
+        return fma(a, b, c, dtype)
+    with np.errstate(all="ignore"):
+        return dtype(dtype(c) + dtype(dtype(a) * dtype(b)))
+
+
+def time_to_next_pixel(vel, frac, dtype, variant=DEFAULT_VARIANT):
+    """src/lib.rs:157-180, all four feature builds."""
     one, half = dtype(1.0), dtype(0.5)
     with np.errstate(all="ignore"):
-        rem = fma(one + signum(vel, dtype), half - frac, frac, dtype)
+        if not variant & VARIANT_BRANCHLESS:
+            if vel > 0:
+                return dtype((one - frac) / vel)
+            if vel < 0:
+                return dtype(-(frac / vel))
+            return dtype(np.inf)
+        rem = mul_add(one + signum(vel, dtype), dtype(half - frac), frac, dtype, variant)
         return dtype(abs(rem / vel))
 
 
-def advance(u, v, i, j, fx, fy, bounds, dtype):
+def advance(u, v, i, j, fx, fy, bounds, dtype, variant=DEFAULT_VARIANT):
     """src/lib.rs:236-273; bounds = ((xl, xr), (yl, yr), nx, ny), names as str."""
     if u == 0 and v == 0:
         return i, j, fx, fy
-    tx = time_to_next_pixel(u, fx, dtype)
-    ty = time_to_next_pixel(v, fy, dtype)
+    tx = time_to_next_pixel(u, fx, dtype, variant)
+    ty = time_to_next_pixel(v, fy, dtype, variant)
     if tx < ty:
         if u >= 0:
             j, fx = j + 1, dtype(0.0)
         else:
             j, fx = j - 1, dtype(1.0)
-        fy = fma(tx, v, fy, dtype)
+        fy = mul_add(tx, v, fy, dtype, variant)
     else:
         if v >= 0:
             i, fy = i + 1, dtype(0.0)
         else:
             i, fy = i - 1, dtype(1.0)
-        fx = fma(ty, u, fx, dtype)
+        fx = mul_add(ty, u, fx, dtype, variant)
     (xl, xr), (yl, yr), nx, ny = bounds
     j = _apply(j, xl, xr, nx)
     i = _apply(i, yl, yr, ny)
@@ -108,7 +130,7 @@ def _apply(c, left, right, size):
 
 
 def convolve(texture, u, v, kernel, uv_mode="velocity", boundaries=(("closed",) * 2,) * 2,
-             iterations=1):
+             iterations=1, variant=DEFAULT_VARIANT):
     """src/lib.rs:305-443 on tiny arrays; boundaries as ((xl, xr), (yl, yr))."""
     dtype = texture.dtype.type
     ny, nx = texture.shape
@@ -121,7 +143,7 @@ def convolve(texture, u, v, kernel, uv_mode="velocity", boundaries=(("closed",) 
         out = np.zeros_like(inp)
         for i0 in range(ny):
             for j0 in range(nx):
-                acc = fma(kernel[kmid], inp[i0, j0], dtype(0.0), dtype)
+                acc = mul_add(kernel[kmid], inp[i0, j0], dtype(0.0), dtype, variant)
                 for backward in (False, True):
                     i, j = i0, j0
                     fx = fy = dtype(0.5)
@@ -138,8 +160,8 @@ def convolve(texture, u, v, kernel, uv_mode="velocity", boundaries=(("closed",) 
                             lu, lv = pu, pv
                         if backward:
                             pu, pv = -pu, -pv
-                        i, j, fx, fy = advance(pu, pv, i, j, fx, fy, bounds, dtype)
-                        acc = fma(kernel[k], inp[i, j], acc, dtype)
+                        i, j, fx, fy = advance(pu, pv, i, j, fx, fy, bounds, dtype, variant)
+                        acc = mul_add(kernel[k], inp[i, j], acc, dtype, variant)
                 out[i0, j0] = acc
         inp = out
     return out

@@ -7,7 +7,7 @@ Three sources, none of which needs a GPU:
 * the exact identities its Python suite asserts on outputs
   (tests/test_convolution.py:42-206), evaluated here on the oracle;
 * an independent pure-Python restatement (oracle/pyoracle.py) on tiny
-  images, which must agree bit for bit;
+  images, which must agree bit for bit in all four Cargo feature builds;
 * committed golden vectors (tests/golden/), which must reproduce exactly on
   every host the oracle is built on.
 """
@@ -243,12 +243,54 @@ def _tiny_cases():
                 yield tex, u, v, k, mode, bnd
 
 
+@pytest.mark.parametrize("variant", [3, 2, 1, 0], ids=["fma-branchless", "branchless",
+                                                      "fma", "plain"])
 @pytest.mark.parametrize("case", list(_tiny_cases()))
-def test_oracle_matches_python_restatement(oracle, case) -> None:
+def test_oracle_matches_python_restatement(oracle, case, variant) -> None:
+    # every Cargo feature build of the reference (Cargo.toml:27-30)
     tex, u, v, k, mode, bnd = case
-    want = pyoracle.convolve(tex, u, v, k, mode, bnd, iterations=2)
-    got = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries=bnd, iterations=2)
+    want = pyoracle.convolve(tex, u, v, k, mode, bnd, iterations=2, variant=variant)
+    got = oracle.convolve(tex, u, v, k, uv_mode=mode, boundaries=bnd, iterations=2,
+                          variant=variant)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_time_to_next_pixel_variants_match_python_restatement(oracle, dtype) -> None:
+    # src/lib.rs:157-180 in all four builds, bit for bit, on random velocities
+    # over twelve decades (signed zeros included) and fractions in [0, 1]
+    rng = np.random.default_rng(12)
+    n = 1200
+    vel = ((rng.random(n) - 0.5) * 10.0 ** rng.integers(-6, 6, n)).astype(dtype)
+    vel[:4] = (0.0, -0.0, 1e-30, -1e30)
+    frac = rng.random(n).astype(dtype)
+    frac[4:40], frac[40:76], frac[76:96] = 0.0, 1.0, 0.5
+    frac[96:900] *= dtype(0.3)  # f < 1/4 with a full significand: 0.5 - f inexact
+    differs = 0
+    for x, f in zip(vel, frac):
+        got = [oracle.time_to_next_pixel(float(x), float(f), dtype, variant=var)
+               for var in range(4)]
+        for var in range(4):
+            want = pyoracle.time_to_next_pixel(x, f, dtype, var)
+            assert np.asarray(got[var], dtype).tobytes() == np.asarray(want, dtype).tobytes(), (
+                x, f, var)
+        differs += got[0] != got[3]
+    # the branchy and branchless forms round differently on some inputs
+    assert differs > 0
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_fma_feature_changes_outputs(oracle, dtype) -> None:
+    # with and without `fma` the accumulation rounds differently (src/lib.rs:353-360)
+    rng = np.random.default_rng(11)
+    n = 24
+    tex = rng.random((n, n)).astype(dtype)
+    u = (rng.random((n, n)) - 0.5).astype(dtype)
+    v = (rng.random((n, n)) - 0.5).astype(dtype)
+    k = rng.random(15).astype(dtype)
+    outs = [oracle.convolve(tex, u, v, k, variant=var) for var in range(4)]
+    assert not np.array_equal(outs[3], outs[2])
+    assert not np.array_equal(outs[1], outs[0])
 
 
 def test_python_fma_single_rounding() -> None:
