@@ -200,6 +200,22 @@ class ClockSampler:
         }
 
 
+# ------------------------------------------------------------ roofline --
+
+def compulsory_roofline(px: int, iters: int, elem: int, ms_step: float, peak: float) -> dict:
+    """The compulsory-traffic figure of a whole step.
+
+    Whatever the caches do, every pass reads the texture, u and v and writes
+    its output once: 4 * elem bytes per pixel per iteration (16 B for
+    float32).  Its rate over the measured step time bounds how far below
+    the HBM roofline a step sits if nothing were re-read.
+    """
+    nbytes = 4 * elem * px * iters
+    gbs = nbytes / (ms_step / 1e3) / 1e9
+    return {"bytes_per_px_per_iter": 4 * elem, "bytes_per_step": nbytes,
+            "achieved": gbs, "unit": "GB/s", "frac": gbs / peak}
+
+
 # -------------------------------------------------------------- CPU legs --
 
 def cpu_sample(case_np: dict, seconds: float, threads: int) -> dict:
@@ -482,6 +498,7 @@ def run_gb300(args, dist: Dist) -> None:
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg[dominant] * px,
                 "launch_ms": times[dominant],
+                "compulsory": compulsory_roofline(px, ITERS, 4, ms_step, peak),
             },
             "kernels": kernels,
             "forms": {
