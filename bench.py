@@ -130,19 +130,33 @@ class Dist:
 # ---------------------------------------------------------------- clocks --
 
 class ClockSampler:
-    """nvidia-smi samples every 100 ms while the timed region runs."""
+    """nvidia-smi samples every 100 ms while the timed region runs.
+
+    Entering starts nvidia-smi and returns once its first sample is written
+    (or after STARTUP_S), so that a short timed region is not over before
+    sampling begins; the samples written up to then precede the region and
+    are left out of the summary (used only when none falls inside it).
+    """
 
     FIELDS = ("pci.bus_id,clocks.sm,clocks.max.sm,power.draw,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
     REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+    STARTUP_S = 5.0
 
     def __init__(self, pci: tuple[int, int, int] | None) -> None:
         self.pci = pci
         self.proc = None
+        self.skip = 0
         fd, name = tempfile.mkstemp(prefix="rlic_clocks_", suffix=".csv")
         os.close(fd)
         self.path = Path(name)
+
+    def _complete_lines(self) -> int:
+        try:
+            return self.path.read_text().count("\n")
+        except OSError:
+            return 0
 
     def __enter__(self):
         try:
@@ -152,6 +166,12 @@ class ClockSampler:
                  "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return self
+        deadline = time.monotonic() + self.STARTUP_S
+        while (time.monotonic() < deadline and self.proc.poll() is None
+               and self._complete_lines() == 0):
+            time.sleep(0.02)
+        self.skip = self._complete_lines()
         return self
 
     def __exit__(self, *exc) -> None:
@@ -174,9 +194,14 @@ class ClockSampler:
     def summary(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        rows = [[x.strip() for x in line.split(",")]
-                for line in self.path.read_text().splitlines()]
+        lines = self.path.read_text().splitlines()
         self.path.unlink(missing_ok=True)
+        window = "timed region"
+        if len(lines) > self.skip:
+            lines = lines[self.skip:]
+        elif lines:
+            window = "just before the timed region (none fell inside it)"
+        rows = [[x.strip() for x in line.split(",")] for line in lines]
         rows = [r for r in rows if len(r) == 8]
         if self.pci is not None and any(self._pci(r[0]) == self.pci for r in rows):
             rows = [r for r in rows if self._pci(r[0]) == self.pci]
@@ -197,6 +222,7 @@ class ClockSampler:
             "sm_max_mhz": max(smax) if smax else None,
             "reasons": reasons,
             "samples": len(rows),
+            "window": window,
         }
 
 

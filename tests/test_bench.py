@@ -3,6 +3,10 @@ the workload description and the parsing of nvidia-smi clock samples."""
 
 from __future__ import annotations
 
+import os
+import textwrap
+import time
+
 import pytest
 
 import bench
@@ -68,3 +72,54 @@ def test_clock_summary_without_samples() -> None:
     clocks = bench.ClockSampler(None)
     assert clocks.summary()["reasons"] == ["nvidia-smi unavailable"]
     clocks.path.unlink(missing_ok=True)
+
+
+_ROW = "00000009:01:00.0, {mhz}, 2070, 900, Not Active, Not Active, Not Active, Not Active"
+
+
+def _fake_smi(tmp_path, monkeypatch, body: str) -> None:
+    """An executable named nvidia-smi, first on PATH, running `body`."""
+    exe = tmp_path / "nvidia-smi"
+    exe.write_text("#!/usr/bin/env python3\n" + textwrap.dedent(body))
+    exe.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+
+
+def test_sampler_starts_before_the_region_and_skips_earlier_samples(tmp_path, monkeypatch):
+    # the first sample (idle clock) precedes the region; later ones are under load
+    _fake_smi(tmp_path, monkeypatch, f"""
+        import time
+        k = 0
+        while True:
+            print({_ROW!r}.format(mhz=1000 if k == 0 else 2070), flush=True)
+            k += 1
+            time.sleep(0.05)
+    """)
+    with bench.ClockSampler(None) as clocks:
+        assert clocks.skip >= 1
+        time.sleep(0.4)
+    s = clocks.summary()
+    assert s["window"] == "timed region"
+    assert s["sm_mhz"] == 2070 and s["samples"] >= 2
+
+
+def test_sampler_falls_back_to_samples_before_a_short_region(tmp_path, monkeypatch):
+    _fake_smi(tmp_path, monkeypatch, f"""
+        import time
+        print({_ROW!r}.format(mhz=1980), flush=True)
+        time.sleep(60)
+    """)
+    with bench.ClockSampler(None) as clocks:
+        time.sleep(0.05)
+    s = clocks.summary()
+    assert s["window"].startswith("just before")
+    assert s["sm_mhz"] == 1980 and s["samples"] == 1
+
+
+def test_sampler_does_not_wait_for_a_silent_exit(tmp_path, monkeypatch):
+    _fake_smi(tmp_path, monkeypatch, "raise SystemExit(9)\n")
+    t0 = time.monotonic()
+    with bench.ClockSampler(None) as clocks:
+        pass
+    assert time.monotonic() - t0 < bench.ClockSampler.STARTUP_S
+    assert clocks.summary()["reasons"] == ["no samples"]
