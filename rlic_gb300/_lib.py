@@ -154,6 +154,16 @@ def _element_strides(a: np.ndarray) -> tuple[int, int] | None:
     return a.strides[0] // its, a.strides[1] // its
 
 
+def _empty_result(shape: tuple[int, ...], dtype: np.dtype) -> np.ndarray:
+    """The result for an image without pixels (a zero-length axis).
+
+    The native core allocates its zero-filled output and its pixel loops
+    run zero times, so any kernel, even an empty one, gives a new empty
+    array of the input's shape (src/lib.rs:364-375, 424-442).
+    """
+    return np.zeros(shape, dtype=dtype)
+
+
 def _convolve_numpy(
     texture: np.ndarray,
     u: np.ndarray,
@@ -165,6 +175,8 @@ def _convolve_numpy(
 ) -> np.ndarray:
     lib = _native.lib()
     dtype = texture.dtype
+    if texture.size == 0:
+        return _empty_result(texture.shape, dtype)
     k_c = np.ascontiguousarray(kernel)
     ny, nx = texture.shape
     # a page-locked result buffer, reused once the caller drops an earlier one
@@ -220,6 +232,8 @@ def _convolve_torch(
             "torch inputs must be CUDA tensors on one device. "
             f"Got texture.device={texture.device}, u.device={u.device}, v.device={v.device}"
         )
+    if texture.numel() == 0:
+        return torch.zeros(tuple(texture.shape), dtype=texture.dtype, device=dev)
     with torch.cuda.device(dev):
         tex_c = texture.contiguous()
         u_c = u.contiguous()

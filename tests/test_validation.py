@@ -164,6 +164,20 @@ def test_zero_iterations_returns_new_copy() -> None:
     assert out is not t and not np.shares_memory(out, t)
 
 
+@pytest.mark.parametrize("shape", [(0, 5), (7, 0), (0, 0)])
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("klen", [0, 3])
+def test_image_without_pixels_gives_an_empty_result(shape, dtype, klen) -> None:
+    # the native core's pixel loops run zero times (src/lib.rs:373-374), so the
+    # call returns a new empty array, even for an empty kernel; needs the
+    # library (loaded, never launched), not a GPU
+    t = np.zeros(shape, dtype=dtype)
+    out = rlic.convolve(t, t, t, kernel=np.ones(klen, dtype=dtype), iterations=3,
+                        uv_mode="polarization", boundaries="periodic")
+    assert out.shape == shape and out.dtype == np.dtype(dtype)
+    assert out is not t
+
+
 def test_alias_modules_match_package() -> None:
     import rlic._boundaries
     import rlic._typing
