@@ -172,7 +172,11 @@ def _convolve_numpy(
     uv_code: int,
     bcodes: tuple[int, int, int, int],
     iterations: int,
+    check_texture: bool = True,
 ) -> np.ndarray:
+    """One call of the C ABI on host arrays.  With check_texture the GPU
+    also scans the texture for negative elements (the reference's
+    validation), and a negative texture raises ValueError."""
     lib = _native.lib()
     dtype = texture.dtype
     if texture.size == 0:
@@ -181,7 +185,9 @@ def _convolve_numpy(
     ny, nx = texture.shape
     # a page-locked result buffer, reused once the caller drops an earlier one
     out = _native.pinned_empty((ny, nx), dtype)
-    flags = _native.RLIC_FLAG_HOST_MEMORY | _native.RLIC_FLAG_CHECK_TEXTURE
+    flags = _native.RLIC_FLAG_HOST_MEMORY
+    if check_texture:
+        flags |= _native.RLIC_FLAG_CHECK_TEXTURE
     f32 = dtype == np.dtype("float32")
     views = (texture, u, v)
     strides = [_element_strides(a) for a in views]
@@ -204,7 +210,7 @@ def _convolve_numpy(
             *bcodes, iterations, _ptr(out), None, 0, None, flags,
         )
     if rc == _native.RLIC_ERR_NEGATIVE_TEXTURE or (
-        rc != _native.RLIC_OK and np.any(texture < 0)
+        rc != _native.RLIC_OK and check_texture and np.any(texture < 0)
     ):
         # the only problem left (every other check passed on the host); it
         # takes precedence over a failure of the native call, as validation
