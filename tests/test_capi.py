@@ -23,6 +23,12 @@ def test_header_declares_the_binding_table() -> None:
     assert sorted(declared_symbols()) == sorted(_native.SIGNATURES)
 
 
+def test_integration_guide_lists_every_entry_point() -> None:
+    guide = (HEADER.parents[1] / "INTEGRATION.md").read_text()
+    for name in declared_symbols():
+        assert f"`{name}`" in guide or f"`{name[:-4]}" in guide, name
+
+
 def test_library_exports_every_declared_symbol(native) -> None:
     for name in declared_symbols():
         assert hasattr(native, name), name
