@@ -263,12 +263,19 @@ RLIC_API int rlic_convolve_lowp_f64(const double *texture, const double *u, cons
  * klen, iterations, 4, flags) exceeds that size fails with
  * RLIC_ERR_WORKSPACE_TOO_SMALL before touching the GPU;
  * RLIC_FLAG_NO_PATH_CACHE shrinks the need to about 12 bytes per pixel.
- * RLIC_FLAG_HOST_MEMORY is rejected.
+ * Zero iterations only clear `out` and have no size limit.
+ * RLIC_FLAG_HOST_MEMORY and RLIC_FLAG_CHECK_TEXTURE are rejected
+ * (RLIC_ERR_INVALID_ARGUMENT).
  *
- * The array belongs to the library's module, so every GPU that loads the
- * library holds it until the process exits.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls
+ * The array belongs to the library's module: once mapped on a GPU it stays
+ * there until the process exits.  Under CUDA's default lazy module loading
+ * it is mapped by the first call on each device, not when the library is
+ * loaded, so that first call is the one that can fail for lack of device
+ * memory (RLIC_ERR_OUT_OF_MEMORY, with a message saying so): make one
+ * warm-up call per device up front, while memory is free.  The first call
+ * on a device also looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls
  * share the one array: calls whose work overlaps on the GPU (different
  * streams, or different host threads on one device) race and must be
  * serialised by the caller.  Each call writes every part of the array it

@@ -162,30 +162,6 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 #define RLIC_HOST_CHUNKS 8
 #endif
 
-// A device word that stays zero: the "no NaN sample" flag of fields the
-// caller vouches for (RLIC_FLAG_FIELD_NAN_FREE).
-__device__ unsigned g_zero_flag = 0u;
-
-const unsigned* zero_flag(cudaError_t* err) {
-    static std::mutex mu;
-    static const unsigned* addr[64] = {};
-    int dev = 0;
-    *err = cudaGetDevice(&dev);
-    if (*err != cudaSuccess) return nullptr;
-    if (dev < 0 || dev >= 64) {
-        *err = cudaErrorInvalidDevice;
-        return nullptr;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        *err = cudaGetSymbolAddress(&p, g_zero_flag);
-        if (*err != cudaSuccess) return nullptr;
-        addr[dev] = static_cast<const unsigned*>(p);
-    }
-    return addr[dev];
-}
-
 // A non-blocking stream per device for the uploads of host-memory calls, at
 // the greatest priority: the block scheduler then gives the upload kernels
 // the SM slots that the traced pass's blocks free, instead of queueing them
@@ -698,7 +674,7 @@ int sweep_impl(const T* tex_in, const void* uv, int64_t ny, int64_t nx, const T*
     LaunchConfig lc = launch_config();
     if (flags & RLIC_FLAG_FIELD_NAN_FREE) {
         cudaError_t e = cudaSuccess;
-        lc.field_nan = zero_flag(&e);
+        lc.field_nan = rlic::zero_flag(&e);
         if (!lc.field_nan) return cuda_fail(e, "cudaGetSymbolAddress");
     }
     RLIC_CUDA_TRY(rlic::launch_pass(var,
@@ -1033,8 +1009,19 @@ int static_scratch(unsigned char** ptr) {
         return fail(RLIC_ERR_INVALID_ARGUMENT, "device ordinal out of range for static scratch");
     std::lock_guard<std::mutex> lock(g_static_mu);
     if (g_static_ptr[dev] == nullptr) {
+        // With lazy module loading (CUDA's default) this lookup is what loads
+        // the module and maps the array on this device, so it can run out of
+        // memory here, once, on the first call.
         void* p = nullptr;
-        RLIC_CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e == cudaErrorMemoryAllocation)
+            return fail(RLIC_ERR_OUT_OF_MEMORY,
+                        "mapping the " + std::to_string(kStaticScratchBytes >> 20) +
+                            " MiB static scratch of rlic_convolve_f32_noalloc on device " +
+                            std::to_string(dev) +
+                            " failed: out of device memory (make the first call on each "
+                            "device early, while memory is free)");
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
         g_static_ptr[dev] = p;
     }
     *ptr = static_cast<unsigned char*>(g_static_ptr[dev]);
@@ -1052,9 +1039,20 @@ int convolve_noalloc_f32(const float* texture, const float* u, const float* v, i
     if (flags & RLIC_FLAG_HOST_MEMORY)
         return fail(RLIC_ERR_INVALID_ARGUMENT,
                     "rlic_convolve_f32_noalloc takes device pointers only");
+    // the texture check belongs to host-memory calls; refusing it here keeps a
+    // caller from believing a check ran
+    if (flags & RLIC_FLAG_CHECK_TEXTURE)
+        return fail(RLIC_ERR_INVALID_ARGUMENT,
+                    "rlic_convolve_f32_noalloc does not check the texture "
+                    "(RLIC_FLAG_CHECK_TEXTURE applies to host-memory calls)");
     if (iterations < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "iterations must be >= 0");
     if (!texture || !u || !v || !kernel || !out)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    // zero passes only clear `out` and touch no scratch: no size limit
+    if (iterations == 0)
+        return run_device<float>(texture, u, v, ny, nx, kernel, klen,
+                                 make_variant(flags, uv_mode), bnd, iterations, out, nullptr,
+                                 flags, static_cast<cudaStream_t>(stream_));
     const WorkspaceLayout wl = workspace_layout(ny, nx, klen, iterations, sizeof(float), flags);
     if (wl.total > kStaticScratchBytes)
         return fail(RLIC_ERR_WORKSPACE_TOO_SMALL,

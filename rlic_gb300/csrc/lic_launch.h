@@ -51,6 +51,11 @@ constexpr int kStorageBF16 = 1;
 // Counts one kernel launch (rlic_kernel_launch_count).
 void count_launch();
 
+// Device address of a word that stays zero (lic_kernels_f32.cu), resolved
+// once per device with that device current: the NaN flag of a field the
+// caller promises holds no NaN sample.
+const unsigned* zero_flag(cudaError_t* err);
+
 // 32-bit words of step codes per pixel for a kernel of klen taps (8 steps of
 // 4 bits per word, forward and backward halves padded separately).
 inline int64_t code_words_per_pixel(int64_t klen) {
