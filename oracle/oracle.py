@@ -143,6 +143,43 @@ def sweep_rows(texture, u, v, kernel, row0, row1, *, uv_mode="velocity", boundar
     return out
 
 
+def convolve_rows(texture, u, v, kernel, row0, row1, *, uv_mode="velocity",
+                  boundaries="closed", iterations=1, variant=DEFAULT_VARIANT,
+                  nthreads=1) -> np.ndarray:
+    """Rows [row0, row1) of ``convolve(..., iterations)``, computed exactly from
+    bands of rows.
+
+    A streamline moves at most klen // 2 rows away from its pixel (one cell
+    per step, src/lib.rs:325-329), so rows [row0, row1) of pass p depend only
+    on rows [row0 - r, row1 + r) of pass p - 1, r = klen // 2.  Pass p is
+    therefore evaluated on rows [row0 - (n - p) r, row1 + (n - p) r) only.
+    With a closed y axis the band is clipped to the image (no streamline
+    crosses a closed edge); with a periodic one, a band that would cross the
+    seam is widened to the whole image.  Rows outside each band hold NaN, so
+    that a read outside it would show in the result.
+    """
+    dtype = np.asarray(texture).dtype
+    tex = np.ascontiguousarray(texture, dtype=dtype)
+    ny, nx = tex.shape
+    if iterations <= 0:
+        return np.zeros((row1 - row0, nx), dtype=dtype)
+    r = int(np.asarray(kernel).size) // 2
+    yl, yr = _bcodes(boundaries)[2:]
+    periodic_y = BOUNDARY_CODES["periodic"] in (yl, yr)
+    cur = tex
+    for p in range(1, iterations + 1):
+        m = (iterations - p) * r
+        a, b = row0 - m, row1 + m
+        if periodic_y and (a < 0 or b > ny):
+            a, b = 0, ny
+        a, b = max(0, a), min(ny, b)
+        nxt = np.full_like(tex, np.nan)
+        nxt[a:b] = sweep_rows(cur, u, v, kernel, a, b, uv_mode=uv_mode, boundaries=boundaries,
+                              variant=variant, nthreads=nthreads)
+        cur = nxt
+    return cur[row0:row1].copy()
+
+
 def paths(u, v, klen, pix, *, uv_mode="velocity", boundaries="closed",
           variant=DEFAULT_VARIANT) -> np.ndarray:
     """(npix, klen-1) int64 linear cells: forward trace, then backward; -1 after a stop."""

@@ -301,6 +301,31 @@ def test_python_fma_single_rounding() -> None:
     assert np.float32(a * a) - np.float32(1) == np.float32(2.0**-11)
 
 
+# ---------------------------------------------------------- row bands --
+
+@pytest.mark.parametrize("bnd", ["closed", "periodic", {"x": "closed", "y": "periodic"},
+                                 {"x": "periodic", "y": "closed"}], ids=str)
+def test_convolve_rows_equals_full_convolution(oracle, bnd) -> None:
+    """The band evaluation that checks the GPU at full image sizes gives the
+    rows of the full n-pass convolution exactly, at edges and in the middle,
+    for kernels of odd and even length."""
+    rng = np.random.default_rng(31)
+    n = 90
+    tex = rng.random((n, n))
+    u = rng.random((n, n)) - 0.5
+    v = rng.random((n, n)) - 0.5
+    u[rng.random((n, n)) < 0.02] = 0.0
+    v[u == 0.0] = 0.0
+    for klen in (9, 12):
+        k = np.hanning(klen + 2)[1:-1]
+        full = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries=bnd,
+                               iterations=4)
+        for r0, r1 in ((0, 3), (40, 47), (87, 90), (12, 13)):
+            band = oracle.convolve_rows(tex, u, v, k, r0, r1, uv_mode="polarization",
+                                        boundaries=bnd, iterations=4)
+            np.testing.assert_array_equal(band, full[r0:r1])
+
+
 # ------------------------------------------------------------- golden --
 
 def _golden_files():
