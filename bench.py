@@ -68,6 +68,9 @@ def parse_args() -> argparse.Namespace:
                    help="target CPU time of the oracle baseline sample")
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--replay", choices=["auto", "l1", "staged"], default="auto",
+                   help="how replayed passes gather: the library's default, through L1, or "
+                        "from TMA-staged shared-memory boxes")
     p.add_argument("--workload",
                    choices=["fourier", "readme", "precision", "adjoint", "batched", "equalize"],
                    default="fourier",
@@ -80,7 +83,19 @@ def parse_args() -> argparse.Namespace:
     return p.parse_args()
 
 
-def config(n: int) -> dict:
+def _replay_modes():
+    from rlic_gb300 import _native
+
+    return {"auto": _native.RLIC_REPLAY_AUTO, "l1": _native.RLIC_REPLAY_L1,
+            "staged": _native.RLIC_REPLAY_STAGED}
+
+
+# the replay kernel each --replay choice runs in a step (the library's
+# default gathers through L1)
+STEP_REPLAY = {"auto": "l1", "l1": "l1", "staged": "staged"}
+
+
+def config(n: int, replay: str = "auto") -> dict:
     return {
         "workload": f"fourier_vortex_{n}x{n}_f32_hann{KLEN}_polarization_xperiodic_yclosed_n{ITERS}",
         "size": [n, n],
@@ -89,7 +104,9 @@ def config(n: int) -> dict:
         "uv_mode": "polarization",
         "boundaries": {"x": "periodic", "y": "closed"},
         "iterations": ITERS,
-        "form": "path cache (pass 1 traces and records 4-bit step codes, passes 2-5 replay)",
+        "form": "path cache (pass 1 traces and records 4-bit step codes, passes 2-5 replay"
+                + (" from TMA-staged shared-memory boxes)" if STEP_REPLAY[replay] == "staged"
+                   else " through L1)"),
         "l2": "inputs larger than L2 (texture 256 MiB, packed field 512 MiB at 8192^2)",
     }
 
@@ -331,6 +348,7 @@ def run_gb300(args, dist: Dist) -> None:
     dev = torch.device("cuda", dist.local_rank)
     torch.cuda.set_device(dev)
     lib = _native.lib()
+    _native.set_replay_mode(_replay_modes()[args.replay])
     n = args.size
     case = fourier_vortex_case(n=n, device=str(dev), as_numpy=False)
     tex, u, v, k = (case[x].contiguous() for x in ("texture", "u", "v", "kernel"))
@@ -420,8 +438,17 @@ def run_gb300(args, dist: Dist) -> None:
 
     ms_trace_rec = timed(sweep(codes.data_ptr()))
     ms_trace = timed(sweep(None))
-    ms_replay = timed(lambda: _native.check(lib.rlic_replay_f32(
-        tex.data_ptr(), codes.data_ptr(), n, n, k.data_ptr(), KLEN, tmp.data_ptr(), sp, 0)))
+    def replay():
+        _native.check(lib.rlic_replay_f32(
+            tex.data_ptr(), codes.data_ptr(), n, n, k.data_ptr(), KLEN, tmp.data_ptr(), sp,
+            sweep_flags))
+
+    replay_ms = {}
+    for name, mode in (("l1", _native.RLIC_REPLAY_L1), ("staged", _native.RLIC_REPLAY_STAGED)):
+        _native.set_replay_mode(mode)
+        replay_ms[name] = timed(replay)
+    _native.set_replay_mode(_replay_modes()[args.replay])
+    ms_replay = replay_ms[STEP_REPLAY[args.replay]]
     ms_pack = timed(lambda: _native.check(lib.rlic_pack_field_f32(
         u.data_ptr(), v.data_ptr(), n, n, uv.data_ptr(), sp)))
     del uv, tmp, codes
@@ -441,7 +468,9 @@ def run_gb300(args, dist: Dist) -> None:
         "replay": code_b + 4 * KLEN + 4,              # codes + tex per tap + out
         "pack": 16,                                    # u, v in, (u, v) out
     }
+    alg["replay_l1"] = alg["replay_staged"] = alg["replay"]
     times = {"trace_record": ms_trace_rec, "trace": ms_trace, "replay": ms_replay,
+             "replay_l1": replay_ms["l1"], "replay_staged": replay_ms["staged"],
              "pack": ms_pack}
     kernels = {}
     for name, ms in times.items():
@@ -513,7 +542,7 @@ def run_gb300(args, dist: Dist) -> None:
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic (seeded Fourier modes + point vortices, 1% zero cells)",
-            "config": config(n),
+            "config": config(n, args.replay),
             "gpu_launches": int(launches),
             "clocks": clk,
             "e2e": {
@@ -530,7 +559,9 @@ def run_gb300(args, dist: Dist) -> None:
             "roofline": {
                 "bound": "hbm",
                 "kernel": {"trace_record": "lic_pass_kernel<float, fma, branchless, pol, record>",
-                           "replay": "lic_gather_kernel<float, fma>",
+                           "replay": ("lic_gather_staged_kernel<float, fma>"
+                                      if STEP_REPLAY[args.replay] == "staged"
+                                      else "lic_gather_kernel<float, fma>"),
                            "pack": "pack_uv_kernel<float>"}[dominant],
                 "achieved": kernels[dominant]["achieved_gbs"],
                 "peak": peak,

@@ -358,7 +358,10 @@ RLIC_API int rlic_trace_cells_f64(const double *u, const double *v, int64_t ny, 
  * rlic_replay_*: one convolution pass replayed from `codes` recorded by
  *   rlic_sweep_* on the same ny x nx image with the same klen (boundaries
  *   and uv mode are part of the record).  Identical results to
- *   rlic_sweep_*; `flags` takes RLIC_FLAG_NO_FMA only.
+ *   rlic_sweep_*; `flags` takes RLIC_FLAG_NO_FMA and
+ *   RLIC_FLAG_FIELD_NAN_FREE (the codes were recorded from a field without
+ *   NaN samples, so they hold no stop code and none is tested for; codes
+ *   that do hold one then give undefined results).
  */
 RLIC_API int rlic_pack_field_f32(const float *u, const float *v, int64_t ny, int64_t nx,
                                  void *uv, void *stream);
@@ -378,6 +381,34 @@ RLIC_API int rlic_replay_f32(const float *tex_in, const void *codes, int64_t ny,
 RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny, int64_t nx,
                              const double *kernel, int64_t klen, double *tex_out,
                              void *stream, unsigned flags);
+
+/*
+ * How replayed passes (path cache, passes 2..n) gather the texture:
+ *   RLIC_REPLAY_L1      through L1 and L2 (lic_gather_kernel);
+ *   RLIC_REPLAY_STAGED  from a box of cells around each 64 x stage_rows pixel
+ *                       super-tile, copied into shared memory by the Tensor
+ *                       Memory Accelerator; super-tiles whose box crosses a
+ *                       periodic edge, and images that do not fit the form
+ *                       (rows not a multiple of 16 bytes, textures not in
+ *                       device memory or not 16-byte aligned, boxes beyond
+ *                       256 cells a side or the shared memory of a CTA,
+ *                       2^31 pixels or more), use L1;
+ *   RLIC_REPLAY_AUTO    the library's default (L1).
+ * Both give bit-identical results.  stage_rows: super-tile height, a
+ * multiple of 4 in [4, 64], or 0 for 24.  Affects calls made after it on any
+ * thread.  No counterpart in the reference (a tuning knob of this
+ * implementation).
+ */
+#define RLIC_REPLAY_AUTO 0
+#define RLIC_REPLAY_L1 1
+#define RLIC_REPLAY_STAGED 2
+RLIC_API int rlic_set_replay_mode(int mode, int stage_rows);
+/*
+ * 1 if a staged replay ever gave up waiting for one of its copies (each wait
+ * is bounded; the CTA then returns and its remaining pixels are not written),
+ * 0 if not, -1 if the device could not be queried.  Synchronises the device.
+ */
+RLIC_API int rlic_stage_timeouts(void);
 
 /*
  * Launch-shape tuning for the streamline kernels: CTA width and height in

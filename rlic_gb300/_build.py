@@ -49,6 +49,7 @@ SOURCES = [
     "lic_lowp.cu",
     "lic_batch.cu",
     "lic_equalize.cu",
+    "lic_stage.cu",
 ]
 
 

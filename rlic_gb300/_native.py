@@ -40,6 +40,10 @@ RLIC_FLAG_FIELD_NAN_FREE = 0x40
 RLIC_STORAGE_FP16 = 0
 RLIC_STORAGE_BF16 = 1
 
+RLIC_REPLAY_AUTO = 0
+RLIC_REPLAY_L1 = 1
+RLIC_REPLAY_STAGED = 2
+
 # size of the static scratch of rlic_convolve_f32_noalloc (RLIC_NOALLOC_SCRATCH_BYTES)
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -96,6 +100,8 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_equalize_histogram_f32": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_equalize_histogram_f64": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
+    "rlic_set_replay_mode": ([_INT, _INT], _INT),
+    "rlic_stage_timeouts": ([], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
     "rlic_release_cached_memory": ([], _INT),
     "rlic_host_buffer_alloc": ([_SZ], _P),
@@ -192,3 +198,8 @@ def launch_count() -> int:
 
 def set_block_shape(block_x: int, block_y: int) -> None:
     check(lib().rlic_set_block_shape(block_x, block_y))
+
+
+def set_replay_mode(mode: int, stage_rows: int = 0) -> None:
+    """RLIC_REPLAY_AUTO, _L1 or _STAGED for the replayed passes (bit-identical)."""
+    check(lib().rlic_set_replay_mode(mode, stage_rows))

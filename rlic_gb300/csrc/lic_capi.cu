@@ -216,6 +216,31 @@ Variant make_variant(unsigned flags, int uv_mode) {
 
 LaunchConfig launch_config() { return LaunchConfig{g_block_x.load(), g_block_y.load()}; }
 
+// How replayed passes gather (rlic_set_replay_mode).
+std::atomic<int> g_replay_mode{RLIC_REPLAY_AUTO};
+constexpr bool kStagedByDefault = false;
+
+// One replayed pass: from a texture box staged in shared memory by TMA
+// copies when the mode asks for it and the image fits that form (device
+// memory, 16-byte rows), otherwise through L1.
+template <typename T>
+cudaError_t replay_pass(bool fma, const T* src, const uint32_t* codes, const T* kernel, int klen,
+                        const Shape& sh, const LaunchConfig& lc, T* dst, cudaStream_t stream) {
+    const int mode = g_replay_mode.load();
+    if (mode == RLIC_REPLAY_STAGED || (mode == RLIC_REPLAY_AUTO && kStagedByDefault)) {
+        cudaPointerAttributes attr{};
+        const bool device = cudaPointerGetAttributes(&attr, src) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeDevice;
+        cudaGetLastError();  // a host pointer is not an error to keep
+        if (device) {
+            const cudaError_t e = rlic::launch_gather_staged(fma, src, codes, kernel, klen, sh,
+                                                             lc.field_nan, dst, stream);
+            if (e != cudaErrorNotSupported) return e;
+        }
+    }
+    return rlic::launch_gather(fma, src, codes, kernel, klen, sh, lc, dst, stream);
+}
+
 int check_shape(int64_t ny, int64_t nx, int64_t klen) {
     if (ny <= 0 || nx <= 0)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "image dimensions must be positive");
@@ -323,7 +348,7 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
                                             src, uv, kernel, int(klen), sh, lc, dst, codes,
                                             stream));
         } else {
-            RLIC_CUDA_TRY(rlic::launch_gather(var.fma, src, codes, kernel, int(klen), sh, lc,
+            RLIC_CUDA_TRY(replay_pass(var.fma, src, codes, kernel, int(klen), sh, lc,
                                               dst, stream));
         }
         src = dst;
@@ -540,15 +565,18 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
             RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
         const T* src = dst_of(0);
+        // every chunk has arrived: the field's NaN flag is final
+        LaunchConfig later = lc;
+        later.field_nan = nan_flag;
         for (int64_t it = 1; it < iterations; ++it) {
             if (it + 1 == iterations) prefault();
             T* dst = dst_of(it);
             if (cache) {
-                RLIC_CUDA_TRY(rlic::launch_gather(var.fma, src, codes, d_kernel, int(klen), sh,
-                                                  lc, dst, stream));
+                RLIC_CUDA_TRY(replay_pass(var.fma, src, codes, d_kernel, int(klen), sh, later,
+                                          dst, stream));
             } else {
                 RLIC_CUDA_TRY(rlic::launch_pass(var, rlic::kPassSample, src, uvb, d_kernel,
-                                                int(klen), sh, lc, dst, codes, stream));
+                                                int(klen), sh, later, dst, codes, stream));
             }
             src = dst;
         }
@@ -692,17 +720,28 @@ int replay_impl(const T* tex_in, const void* codes, int64_t ny, int64_t nx, cons
     g_last_error.clear();
     int rc = check_shape(ny, nx, klen);
     if (rc) return rc;
-    if (flags & ~unsigned(RLIC_FLAG_NO_FMA))
-        return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes RLIC_FLAG_NO_FMA only");
+    if (flags & ~unsigned(RLIC_FLAG_NO_FMA | RLIC_FLAG_FIELD_NAN_FREE))
+        return fail(RLIC_ERR_INVALID_ARGUMENT,
+                    "this entry point takes RLIC_FLAG_NO_FMA and RLIC_FLAG_FIELD_NAN_FREE only");
     if (!tex_in || !kernel || !tex_out || (!codes && klen > 1))
         return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
     if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
-    const int bnd[4] = {0, 0, 0, 0};
-    RLIC_CUDA_TRY(rlic::launch_gather(!(flags & RLIC_FLAG_NO_FMA), tex_in,
-                                      static_cast<const uint32_t*>(codes), kernel, int(klen),
-                                      make_shape(ny, nx, bnd), launch_config(), tex_out,
-                                      static_cast<cudaStream_t>(stream_)));
+    // the codes may hold wraps across any edge (the boundaries they were
+    // recorded with are not known here): treat every side as periodic, so
+    // that the staged form stages no box that crosses an edge (the L1 form
+    // reads only the image size)
+    const int bnd[4] = {1, 1, 1, 1};
+    LaunchConfig lc = launch_config();
+    if (flags & RLIC_FLAG_FIELD_NAN_FREE) {  // codes recorded from a NaN-free field
+        cudaError_t e = cudaSuccess;
+        lc.field_nan = rlic::zero_flag(&e);
+        if (!lc.field_nan) return cuda_fail(e, "cudaGetSymbolAddress");
+    }
+    RLIC_CUDA_TRY(replay_pass(!(flags & RLIC_FLAG_NO_FMA), tex_in,
+                              static_cast<const uint32_t*>(codes), kernel, int(klen),
+                              make_shape(ny, nx, bnd), lc, tex_out,
+                              static_cast<cudaStream_t>(stream_)));
     return RLIC_OK;
 }
 
@@ -1309,6 +1348,23 @@ int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float*
                               int64_t iterations, float* out, void* stream, unsigned flags) {
     return convolve_noalloc_f32(texture, u, v, ny, nx, kernel, klen, uv_mode, bx_left, bx_right,
                                 by_left, by_right, iterations, out, stream, flags);
+}
+
+int rlic_set_replay_mode(int mode, int stage_rows) {
+    g_last_error.clear();
+    if (mode != RLIC_REPLAY_AUTO && mode != RLIC_REPLAY_L1 && mode != RLIC_REPLAY_STAGED)
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "mode must be RLIC_REPLAY_AUTO, _L1 or _STAGED");
+    if (stage_rows != 0 && (stage_rows < 4 || stage_rows > 64 || stage_rows % 4 != 0))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "stage_rows must be 0 or a multiple of 4 in [4, 64]");
+    g_replay_mode.store(mode);
+    rlic::set_stage_rows(stage_rows ? stage_rows : 24);
+    return RLIC_OK;
+}
+
+int rlic_stage_timeouts(void) {
+    bool seen = false;
+    if (rlic::stage_timeout_seen(&seen) != cudaSuccess) return -1;
+    return seen ? 1 : 0;
 }
 
 int rlic_set_block_shape(int block_x, int block_y) {

@@ -108,6 +108,25 @@ cudaError_t launch_gather_lowp(int storage, const void* tex_in, const uint32_t* 
                                const Shape& sh, const LaunchConfig& lc, void* tex_out,
                                cudaStream_t stream);
 
+// Replayed pass with the texture staged in shared memory by TMA copies
+// (lic_stage.cu).  Returns cudaErrorNotSupported, before launching anything,
+// when the image or the kernel does not fit the staged form (rows not
+// 16-byte multiples, an unaligned texture, a box beyond the copy limits,
+// images of 2^31 pixels or more); the caller then uses launch_gather.
+// field_nan: the packed field's NaN flag (null: unknown; codes may then
+// hold stop codes).
+cudaError_t launch_gather_staged(bool fma, const float* tex_in, const uint32_t* codes,
+                                 const float* kernel, int klen, const Shape& sh,
+                                 const unsigned* field_nan, float* tex_out, cudaStream_t stream);
+cudaError_t launch_gather_staged(bool fma, const double* tex_in, const uint32_t* codes,
+                                 const double* kernel, int klen, const Shape& sh,
+                                 const unsigned* field_nan, double* tex_out,
+                                 cudaStream_t stream);
+// Super-tile height of the staged replay, in pixels (a multiple of 4).
+void set_stage_rows(int rows);
+// Whether a staged replay ever gave up waiting for its copy.
+cudaError_t stage_timeout_seen(bool* seen);
+
 // Self-check of the screened float64 division (lic_kernels_f64.cu).
 cudaError_t launch_quotient_check(const double* a, const double* b, int64_t n, double* q,
                                   int32_t* certified, cudaStream_t stream);

@@ -1,0 +1,421 @@
+// lic_stage.cu -- the replayed pass with its texture staged in shared memory
+// by the Tensor Memory Accelerator (TMA).
+//
+// A replayed pass (lic_gather_kernel) gathers K texture cells per pixel along
+// the recorded streamline.  Every cell a pixel samples lies within
+// kmid = klen / 2 cells of it along each axis (one cell per step,
+// src/lib.rs:325-329), so a super-tile of SX x SY pixels samples only a box of
+// (SX + 2 HX) x (SY + 2 HY) cells around it, HX >= kmid and HY = kmid.  This
+// kernel is persistent: each CTA loops over super-tiles; for each one a
+// single thread issues one `cp.async.bulk.tensor.2d` copy of the box from HBM
+// (through L2) into shared memory, completing on an mbarrier, and the CTA
+// then replays its pixels from shared memory.  The copy engine fills the box,
+// so the fill costs the load/store pipe nothing; the gathers, which bound the
+// L1-cached replay, become shared-memory loads.
+//
+// Super-tiles whose box would cross a periodic image edge (their streamlines
+// may wrap to the far side) replay through L1/L2 as lic_gather_kernel does.
+// Boxes that cross a closed edge are staged: the copy fills cells outside the
+// image with zeros, and no streamline reaches them (a closed edge clamps).
+// Accumulation order and weights are those of the traced pass, so the results
+// are bit-identical to lic_gather_kernel's.
+//
+// Every wait on the mbarrier is bounded: after kStageWaitLimit polls the CTA
+// sets the library's stage-timeout word and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+#include <mutex>
+
+#include "lic_kernels.cuh"
+
+namespace rlic {
+
+namespace {
+
+constexpr int kStageThreadsX = 64;  // CTA: 64 x 4 threads, one column per thread
+constexpr int kStageThreadsY = 4;
+constexpr int kStageBoxOffset = 128;  // box start in shared memory (after the mbarrier)
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+
+__device__ unsigned g_stage_timeout = 0u;
+
+struct StageGrid {
+    int sx, sy;       // super-tile, pixels
+    int hx, hy;       // halo, cells
+    int bw, bh;       // staged box, cells (bw is the shared-memory row pitch)
+    int tiles_x, ntiles;
+    bool wrap_x, wrap_y;  // an axis with a periodic side
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Polls the barrier's phase `parity` at most kStageWaitLimit times.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (uint32_t k = 0; k < kStageWaitLimit; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// One 2-D tiled copy of the box at (x, y) (elements; x aligned to 16 bytes,
+// negative or out-of-range coordinates read zeros) into shared memory.
+__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, int x, int y,
+                                             uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// The cell offset of step b of a code word inside a staged box of row pitch
+// `pitch`: the column move (bits 4b..4b+1) and the row move (bits
+// 4b+2..4b+3) as signed 2-bit fields.  A staged box never meets the wrap
+// codes, and stop codes are handled before a word gets here, so only
+// 0 / +1 / -1 occur; decoding by arithmetic keeps the gathers the only
+// shared-memory loads of a step.
+__device__ __forceinline__ int box_delta(uint32_t wd, int b, int pitch) {
+    const int dx = int(wd << (30 - 4 * b)) >> 30;
+    const int dy = int(wd << (28 - 4 * b)) >> 30;
+    return dy * pitch + dx;
+}
+
+// The 8 weights of one code word (8-entry aligned in shared memory) with
+// 16-byte loads; every lane reads the same address.
+__device__ __forceinline__ void load_weights8(const float* w, float out[8]) {
+    const float4 a = reinterpret_cast<const float4*>(w)[0];
+    const float4 b = reinterpret_cast<const float4*>(w)[1];
+    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+__device__ __forceinline__ void load_weights8(const double* w, double out[8]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double2 a = reinterpret_cast<const double2*>(w)[k];
+        out[2 * k] = a.x;
+        out[2 * k + 1] = a.y;
+    }
+}
+
+// Word q of one half's codes (0 past the last word of the half).
+__device__ __forceinline__ uint32_t code_word(const uint32_t* __restrict__ words, int64_t npix,
+                                              int q, int nwords) {
+    return q < nwords ? __ldg(words + size_t(q) * size_t(npix)) : 0u;
+}
+
+// The 8 cells of one code word, gathered from the box into x.
+template <typename T>
+__device__ __forceinline__ void gather_word(int& cell, uint32_t wd, int pitch, const T* box,
+                                            T x[8]) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        cell += box_delta(wd, b, pitch);
+        x[b] = box[cell];
+    }
+}
+
+// The 8 ordered kernel-weighted samples of one code word.
+template <typename T, bool FMA>
+__device__ __forceinline__ void accumulate_word(T& acc, const T x[8], const T* w) {
+    T wq[8];
+    load_weights8(w, wq);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
+}
+
+// replay_half (lic_kernels.cuh) on the staged box: the same walk in the
+// traced pass's accumulation order, with shared-memory gathers and
+// arithmetic decoding.  The 8 gathers of word q + 1 are in flight while
+// word q accumulates; the two word buffers alternate, two words per loop
+// turn, so that no register copies are needed.  Code words are loaded two
+// ahead: the caller passes the half's first two words (w0, w1), loaded
+// when the pixel starts, and word q + 2 is requested while word q's
+// gathers are issued.  (Requesting four words ahead measured slower: the
+// extra registers cost a resident CTA.)  STOPS = false: the field holds no
+// NaN sample, so no word holds a stop code and none is tested.
+template <typename T, bool FMA, bool STOPS>
+__device__ __forceinline__ void replay_half_staged(T& acc, int cell,
+                                                   const uint32_t* __restrict__ words,
+                                                   int64_t npix, int count, uint32_t w0,
+                                                   uint32_t w1, const T* w, int pitch,
+                                                   const T* box) {
+    const int full = count >> 3;
+    const int nwords = (count + 7) >> 3;
+    int q = 0;
+    if (full > 0 && !(STOPS && word_has_stop(w0))) {
+        T x[8], y[8];
+        gather_word(cell, w0, pitch, box, x);
+        uint32_t wn = w1;
+        bool in_x = true;  // which buffer holds word q - 1, gathered, not yet accumulated
+        for (q = 1; q < full;) {
+            uint32_t wd = wn;
+            wn = code_word(words, npix, q + 1, nwords);
+            if (STOPS && word_has_stop(wd)) break;
+            gather_word(cell, wd, pitch, box, y);
+            accumulate_word<T, FMA>(acc, x, w + 8 * (q - 1));
+            in_x = false;
+            if (++q >= full) break;
+            wd = wn;
+            wn = code_word(words, npix, q + 1, nwords);
+            if (STOPS && word_has_stop(wd)) break;
+            gather_word(cell, wd, pitch, box, x);
+            accumulate_word<T, FMA>(acc, y, w + 8 * (q - 1));
+            in_x = true;
+            ++q;
+        }
+        if (in_x) {
+            accumulate_word<T, FMA>(acc, x, w + 8 * (q - 1));
+        } else {
+            accumulate_word<T, FMA>(acc, y, w + 8 * (q - 1));
+        }
+    }
+    // a word with a stop code, or the last partial word, step by step
+    for (; q < nwords; ++q) {
+        const int n = (q < full) ? 8 : (count & 7);
+        const uint32_t wd = q == 0 ? w0 : (q == 1 ? w1 : code_word(words, npix, q, nwords));
+        const T* wq = w + 8 * q;
+        for (int b = 0; b < n; ++b) {
+            if (STOPS && ((wd >> (4 * b)) & 15u) == kStop) return;
+            cell += box_delta(wd, b, pitch);
+            acc = accumulate<T, FMA>(wq[b], box[cell], acc);
+        }
+    }
+}
+
+template <typename T, bool FMA>
+__global__ void __launch_bounds__(kStageThreadsX * kStageThreadsY)
+lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __restrict__ tex_in,
+                         const uint32_t* __restrict__ codes, const T* __restrict__ kernel,
+                         int klen, Geometry<int32_t> g, StageGrid sg, T* __restrict__ tex_out,
+                         CodeLayout cl, const unsigned* __restrict__ field_nan) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    T* box = reinterpret_cast<T*>(smem_raw + kStageBoxOffset);
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nf_pad = (nf + 7) & ~7;
+    const int nb_pad = (kmid + 7) & ~7;
+    T* wsm = box + size_t(sg.bw) * size_t(sg.bh);
+    int* gtab = reinterpret_cast<int*>(wsm + nf_pad + nb_pad);  // image deltas
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    load_step_weights(wsm, kernel, klen, nf_pad);
+    if (tid == 0) {
+        fill_delta_table(gtab, g.nx, g.ny);
+        mbar_init(bar);
+    }
+    __syncthreads();
+    const T wmid = __ldg(kernel + kmid);
+    // codes of a field known to hold no NaN sample have no stop code
+    const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
+    const uint32_t* codes_b = codes + size_t(cl.words_f) * size_t(cl.npix);
+    const uint32_t box_bytes = uint32_t(sg.bw) * uint32_t(sg.bh) * uint32_t(sizeof(T));
+    const int nwf = (nf + 7) >> 3, nwb = (kmid + 7) >> 3;
+    uint32_t parity = 0;
+    for (int tile = blockIdx.x; tile < sg.ntiles; tile += gridDim.x) {
+        const int ti = tile / sg.tiles_x;
+        const int tj = tile - ti * sg.tiles_x;
+        const int x0 = tj * sg.sx, y0 = ti * sg.sy;
+        const int bx0 = x0 - sg.hx, by0 = y0 - sg.hy;
+        const bool staged = !(sg.wrap_x && (bx0 < 0 || bx0 + sg.bw > g.nx)) &&
+                            !(sg.wrap_y && (by0 < 0 || by0 + sg.bh > g.ny));
+        if (staged) {
+            if (tid == 0) {
+                // order this CTA's earlier shared-memory reads before the copy
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(bar, box_bytes);
+                tma_load_box(box, &map, bx0, by0, bar);
+            }
+            const bool arrived = mbar_wait_bounded(bar, parity);
+            // the whole CTA leaves together if any thread gave up waiting
+            if (__syncthreads_or(!arrived)) {
+                if (tid == 0) atomicExch(&g_stage_timeout, 1u);
+                if (!arrived) mbar_wait_bounded(bar, parity);  // the copy in flight, once more
+                return;
+            }
+            parity ^= 1u;
+        }
+        for (int r = threadIdx.y; r < sg.sy; r += kStageThreadsY) {
+            const int c = threadIdx.x;
+            const int i = y0 + r, j = x0 + c;
+            if (i >= g.ny || j >= g.nx) continue;
+            const int p = i * g.nx + j;
+            T acc;
+            if (staged) {
+                // both halves' first two code words, four loads in flight
+                const uint32_t f0 = code_word(codes + p, cl.npix, 0, nwf);
+                const uint32_t f1 = code_word(codes + p, cl.npix, 1, nwf);
+                const uint32_t b0 = code_word(codes_b + p, cl.npix, 0, nwb);
+                const uint32_t b1 = code_word(codes_b + p, cl.npix, 1, nwb);
+                const int cell = (r + sg.hy) * sg.bw + (c + sg.hx);
+                acc = accumulate<T, FMA>(wmid, box[cell], T(0));
+                if (nan_free) {
+                    replay_half_staged<T, FMA, false>(acc, cell, codes + p, cl.npix, nf, f0, f1,
+                                                      wsm, sg.bw, box);
+                    replay_half_staged<T, FMA, false>(acc, cell, codes_b + p, cl.npix, kmid, b0,
+                                                      b1, wsm + nf_pad, sg.bw, box);
+                } else {
+                    replay_half_staged<T, FMA, true>(acc, cell, codes + p, cl.npix, nf, f0, f1,
+                                                     wsm, sg.bw, box);
+                    replay_half_staged<T, FMA, true>(acc, cell, codes_b + p, cl.npix, kmid, b0,
+                                                     b1, wsm + nf_pad, sg.bw, box);
+                }
+            } else {
+                acc = accumulate<T, FMA>(wmid, __ldg(tex_in + p), T(0));
+                replay_half<T, FMA, int32_t>(acc, p, codes + p, cl.npix, nf, wsm, gtab, tex_in);
+                replay_half<T, FMA, int32_t>(acc, p, codes_b + p, cl.npix, kmid, wsm + nf_pad,
+                                             gtab, tex_in);
+            }
+            tex_out[p] = acc;
+        }
+        __syncthreads();  // every read of the box precedes the next copy into it
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn(cudaError_t* err) {
+    static std::mutex mu;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        *err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                cudaEnableDefault, &q);
+        if (*err != cudaSuccess) return nullptr;
+        if (q != cudaDriverEntryPointSuccess || !p) {
+            *err = cudaErrorNotSupported;
+            return nullptr;
+        }
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    *err = cudaSuccess;
+    return fn;
+}
+
+int g_stage_rows = 24;  // super-tile height in pixels (a multiple of 4)
+
+// Extra cells per box row (a multiple of 4): a wider box changes the row
+// pitch, and with it which gathers of a warp share a shared-memory bank.
+// RLIC_STAGE_PAD in the environment sets it (tuning only).
+int stage_pad() {
+    static const int pad = [] {
+        const char* e = std::getenv("RLIC_STAGE_PAD");
+        const int v = e ? std::atoi(e) : 0;
+        return (v >= 0 && v <= 64 && v % 4 == 0) ? v : 0;
+    }();
+    return pad;
+}
+
+template <typename T, bool FMA>
+cudaError_t launch_gather_staged_t(const T* tex_in, const uint32_t* codes, const T* kernel,
+                                   int klen, const Shape& sh, const unsigned* field_nan,
+                                   T* tex_out, cudaStream_t stream) {
+    const int kmid = klen / 2;
+    constexpr int align = int(16 / sizeof(T));  // x of a copy: 16-byte aligned
+    if (!sh.small_index() || klen < 2 || (sh.nx * int64_t(sizeof(T))) % 16 != 0 ||
+        (reinterpret_cast<uintptr_t>(tex_in) & 15u) != 0)
+        return cudaErrorNotSupported;
+    StageGrid sg;
+    sg.sx = kStageThreadsX;
+    sg.sy = g_stage_rows;
+    sg.hx = (kmid + align - 1) / align * align;
+    sg.hy = kmid;
+    sg.bw = sg.sx + 2 * sg.hx + stage_pad();
+    sg.bh = sg.sy + 2 * sg.hy;
+    if (sg.bw > 256 || sg.bh > 256) return cudaErrorNotSupported;  // box limit of a copy
+    sg.tiles_x = int(tiles_of(sh.nx, sg.sx));
+    const int64_t ntiles = int64_t(sg.tiles_x) * tiles_of(sh.ny, sg.sy);
+    if (ntiles > 0x7fffffffLL) return cudaErrorNotSupported;
+    sg.ntiles = int(ntiles);
+    sg.wrap_x = sh.bnd[0] == 1 || sh.bnd[1] == 1;
+    sg.wrap_y = sh.bnd[2] == 1 || sh.bnd[3] == 1;
+    const int nf = klen - kmid - 1;
+    const size_t smem = kStageBoxOffset + sizeof(T) * size_t(sg.bw) * size_t(sg.bh) +
+                        sizeof(T) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7)) +
+                        16 * sizeof(int);
+    if (smem > 227 * 1024) return cudaErrorNotSupported;
+
+    cudaError_t e = cudaSuccess;
+    auto encode = encode_fn(&e);
+    if (!encode) return e;
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {cuuint64_t(sh.nx), cuuint64_t(sh.ny)};
+    const cuuint64_t strides[1] = {cuuint64_t(sh.nx) * sizeof(T)};
+    const cuuint32_t box[2] = {cuuint32_t(sg.bw), cuuint32_t(sg.bh)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult cr = encode(
+        &map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+        2, const_cast<T*>(tex_in), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return cudaErrorNotSupported;
+
+    auto kfn = lic_gather_staged_kernel<T, FMA>;
+    unsigned grid = 0;
+    e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, ntiles, &grid);
+    if (e != cudaSuccess) return e;
+    const auto g = make_geometry<int32_t>(sh);
+    const auto cl = make_code_layout(sh, klen);
+    kfn<<<grid, dim3(kStageThreadsX, kStageThreadsY), smem, stream>>>(
+        map, tex_in, codes, kernel, klen, g, sg, tex_out, cl, field_nan);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_gather_staged(bool fma, const float* tex_in, const uint32_t* codes,
+                                 const float* kernel, int klen, const Shape& sh,
+                                 const unsigned* field_nan, float* tex_out,
+                                 cudaStream_t stream) {
+    return fma ? launch_gather_staged_t<float, true>(tex_in, codes, kernel, klen, sh, field_nan,
+                                                     tex_out, stream)
+               : launch_gather_staged_t<float, false>(tex_in, codes, kernel, klen, sh, field_nan,
+                                                      tex_out, stream);
+}
+
+cudaError_t launch_gather_staged(bool fma, const double* tex_in, const uint32_t* codes,
+                                 const double* kernel, int klen, const Shape& sh,
+                                 const unsigned* field_nan, double* tex_out,
+                                 cudaStream_t stream) {
+    return fma ? launch_gather_staged_t<double, true>(tex_in, codes, kernel, klen, sh, field_nan,
+                                                      tex_out, stream)
+               : launch_gather_staged_t<double, false>(tex_in, codes, kernel, klen, sh,
+                                                       field_nan, tex_out, stream);
+}
+
+void set_stage_rows(int rows) { g_stage_rows = rows; }
+
+cudaError_t stage_timeout_seen(bool* seen) {
+    unsigned v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_stage_timeout, sizeof(v));
+    *seen = v != 0;
+    return e;
+}
+
+}  // namespace rlic

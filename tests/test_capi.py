@@ -132,6 +132,10 @@ def test_block_shape_validation(native) -> None:
     assert native.rlic_set_block_shape(0, 4) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 64) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 4) == _native.RLIC_OK
+    assert native.rlic_set_replay_mode(7, 0) == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert native.rlic_set_replay_mode(_native.RLIC_REPLAY_STAGED, 6) == \
+        _native.RLIC_ERR_INVALID_ARGUMENT
+    assert native.rlic_set_replay_mode(_native.RLIC_REPLAY_AUTO, 0) == _native.RLIC_OK
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path) -> None:
