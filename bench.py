@@ -91,8 +91,8 @@ def _replay_modes():
 
 
 # the replay kernel each --replay choice runs in a step (the library's
-# default gathers through L1)
-STEP_REPLAY = {"auto": "l1", "l1": "l1", "staged": "staged"}
+# default stages the texture in shared memory)
+STEP_REPLAY = {"auto": "staged", "l1": "l1", "staged": "staged"}
 
 
 def config(n: int, replay: str = "auto") -> dict:

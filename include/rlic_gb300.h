@@ -393,7 +393,7 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
  *                       device memory or not 16-byte aligned, boxes beyond
  *                       256 cells a side or the shared memory of a CTA,
  *                       2^31 pixels or more), use L1;
- *   RLIC_REPLAY_AUTO    the library's default (L1).
+ *   RLIC_REPLAY_AUTO    the library's default (staged, where the image fits).
  * Both give bit-identical results.  stage_rows: super-tile height, a
  * multiple of 4 in [4, 64], or 0 for 24.  Affects calls made after it on any
  * thread.  No counterpart in the reference (a tuning knob of this
