@@ -801,70 +801,88 @@ def run_equalize(args) -> None:
 
 
 def run_batched(args) -> None:
-    """64 instances (rlic_gb300.workloads.batch_case, seed 3): one batched call
-    (and its CUDA-graph replay) against 64 sequential rlic_convolve_f32 calls."""
+    """Two batched mixes (rlic_gb300.workloads.batch_case): the 64-instance
+    workload (sides 256-4096, seed 3) and 256 small instances (sides
+    128-512, seed 5), each with kernels of 17-129 taps and 1-10 iterations.
+    Per mix: the persistent work-queue launch (tuned tiles, also replayed
+    from a CUDA graph), one launch per level, and one rlic_convolve_f32 call
+    per instance in its path-cache and plain forms."""
     import torch
 
     from rlic_gb300 import _native
+    from rlic_gb300._boundaries import BoundarySet
     from rlic_gb300.batch import BatchPlan, autotune_tiles
     from rlic_gb300.workloads import batch_case
 
-    items = batch_case(count=64, seed=3)
-    dev = items[0]["texture"].device
-    stream = torch.cuda.current_stream(dev)
-    sp = ctypes.c_void_p(stream.cuda_stream)
     lib = _native.lib()
-    t0 = time.perf_counter()
-    choice = autotune_tiles(items)
-    tune_s = time.perf_counter() - t0
-    plan = BatchPlan(items)
-    samples = plan.samples()
     steps = max(3, min(args.steps, 10))
-    ms_batch = _time_calls(plan.run, steps, args.warmup, stream)
-    plan.capture()
-    ms_graph = _time_calls(plan.replay, steps, args.warmup, stream)
 
-    seq = []
-    for it, t in zip(items, plan.inputs):
-        ny, nx = t["texture"].shape
-        klen = t["kernel"].shape[0]
-        from rlic_gb300._boundaries import BoundarySet
-
-        bc = BoundarySet.from_spec(it["boundaries"]).codes()
-        out = torch.empty_like(t["texture"])
-        seq.append((t, ny, nx, klen, it["iterations"], _native.UV_MODE_CODES[it["uv_mode"]], bc, out))
-    wsmax = max(lib.rlic_workspace_bytes(ny, nx, klen, n, 4, 0)
-                for _, ny, nx, klen, n, _, _, _ in seq)
-    ws = torch.empty(wsmax, dtype=torch.uint8, device=dev)
-
-    def sequential(flags):
-        def go():
-            for t, ny, nx, klen, n, mode, bc, out in seq:
-                _native.check(lib.rlic_convolve_f32(
-                    t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), ny, nx,
-                    t["kernel"].data_ptr(), klen, mode, *bc, n, out.data_ptr(), ws.data_ptr(),
-                    wsmax, sp, flags))
-        return go
-
-    ms_seq = _time_calls(sequential(0), steps, args.warmup, stream)
-    ms_seq_plain = _time_calls(sequential(_native.RLIC_FLAG_NO_PATH_CACHE), 2, 1, stream)
-    for (_, _, _, _, _, _, _, out), got in zip(seq, plan.outputs):
-        assert torch.equal(out, got), "batched result differs from the sequential calls"
-
-    def gs(ms):
+    def gs(samples, ms):
         return samples / (ms / 1e3) / 1e9
 
+    def measure(items) -> dict:
+        dev = items[0]["texture"].device
+        stream = torch.cuda.current_stream(dev)
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        t0 = time.perf_counter()
+        choice = autotune_tiles(items)
+        tune_s = time.perf_counter() - t0
+        plan = BatchPlan(items)
+        samples = plan.samples()
+        ms_queue = _time_calls(plan.run, steps, args.warmup, stream)
+        assert plan.status(), "a bounded wait of the work queue gave up"
+        plan.capture()
+        ms_graph = _time_calls(plan.replay, steps, args.warmup, stream)
+        levels = BatchPlan(items, per_level=True)
+        ms_levels = _time_calls(levels.run, steps, args.warmup, stream)
+        seq = []
+        for it, t in zip(items, plan.inputs):
+            ny, nx = t["texture"].shape
+            bc = BoundarySet.from_spec(it["boundaries"]).codes()
+            seq.append((t, ny, nx, t["kernel"].shape[0], it["iterations"],
+                        _native.UV_MODE_CODES[it["uv_mode"]], bc, torch.empty_like(t["texture"])))
+        wsmax = max(lib.rlic_workspace_bytes(ny, nx, klen, n, 4, 0)
+                    for _, ny, nx, klen, n, _, _, _ in seq)
+        ws = torch.empty(wsmax, dtype=torch.uint8, device=dev)
+
+        def sequential(flags):
+            def go():
+                for t, ny, nx, klen, n, mode, bc, out in seq:
+                    _native.check(lib.rlic_convolve_f32(
+                        t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), ny, nx,
+                        t["kernel"].data_ptr(), klen, mode, *bc, n, out.data_ptr(),
+                        ws.data_ptr(), wsmax, sp, flags))
+            return go
+
+        ms_seq = _time_calls(sequential(0), steps, args.warmup, stream)
+        ms_seq_plain = _time_calls(sequential(_native.RLIC_FLAG_NO_PATH_CACHE), 2, 1, stream)
+        for (_, _, _, _, _, _, _, out), a, b in zip(seq, plan.outputs, levels.outputs):
+            assert torch.equal(out, a) and torch.equal(out, b), "batched result differs"
+        return {
+            "instances": len(items),
+            "pixels": int(sum(int(i["texture"].numel()) for i in items)),
+            "samples_per_step": samples,
+            "forms": {
+                "queue_graph_replay": {"ms": ms_graph, "value": gs(samples, ms_graph)},
+                "queue_call": {"ms": ms_queue, "value": gs(samples, ms_queue)},
+                "per_level_call": {"ms": ms_levels, "value": gs(samples, ms_levels)},
+                "sequential_path_cache_calls": {"ms": ms_seq, "value": gs(samples, ms_seq)},
+                "sequential_plain_calls": {"ms": ms_seq_plain,
+                                           "value": gs(samples, ms_seq_plain)},
+            },
+            "autotune": {"seconds": tune_s,
+                         "choices": {str(k): list(v) for k, v in choice.items()}},
+        }
+
+    mixes = {
+        "batch_64_instances_seed3": measure(batch_case(count=64, seed=3)),
+        "batch_256_small_instances_seed5": measure(
+            batch_case(count=256, seed=5, min_side=128, max_side=512)),
+    }
+    head = mixes["batch_64_instances_seed3"]["forms"]["queue_graph_replay"]["value"]
     print(json.dumps({
         "metric": METRIC, "unit": UNIT, "workload": "batch_64_instances_seed3",
-        "value": gs(ms_graph), "dtype": "f32", "samples_per_step": samples,
-        "pixels": int(sum(int(i["texture"].numel()) for i in items)),
-        "forms": {
-            "batched_graph_replay": {"ms": ms_graph, "value": gs(ms_graph)},
-            "batched_call": {"ms": ms_batch, "value": gs(ms_batch)},
-            "sequential_path_cache_calls": {"ms": ms_seq, "value": gs(ms_seq)},
-            "sequential_plain_calls": {"ms": ms_seq_plain, "value": gs(ms_seq_plain)},
-        },
-        "autotune": {"seconds": tune_s, "choices": {str(k): v for k, v in choice.items()}},
+        "value": head, "dtype": "f32", "mixes": mixes,
     }), flush=True)
 
 

@@ -36,6 +36,7 @@ RLIC_FLAG_NO_BRANCHLESS = 0x4
 RLIC_FLAG_NO_PATH_CACHE = 0x8
 RLIC_FLAG_CHECK_TEXTURE = 0x20
 RLIC_FLAG_FIELD_NAN_FREE = 0x40
+RLIC_FLAG_BATCH_PER_LEVEL = 0x80
 
 RLIC_STORAGE_FP16 = 0
 RLIC_STORAGE_BF16 = 1
@@ -94,6 +95,7 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_kernel_grad_f64": ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _U], _INT),
     "rlic_batch_workspace_bytes_f32": ([_P, _INT], _SZ),
     "rlic_convolve_batch_f32": ([_P, _INT, _P, _SZ, _P, _U], _INT),
+    "rlic_batch_status_f32": ([_P, _INT, _P], _INT),
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_check_quotients_f64": ([_P, _P, _I64, _P, _P, _P], _INT),
@@ -119,6 +121,7 @@ class BatchItemF32(ctypes.Structure):
         ("iterations", ctypes.c_int64),
         ("uv_mode", ctypes.c_int), ("bx_left", ctypes.c_int), ("bx_right", ctypes.c_int),
         ("by_left", ctypes.c_int), ("by_right", ctypes.c_int), ("tile_x", ctypes.c_int),
+        ("replay_tiles", ctypes.c_int),
     ]
 
 

@@ -4,16 +4,21 @@
 ``convolve``: ``texture``, ``u``, ``v``, ``kernel`` as float32 CUDA tensors,
 plus ``uv_mode``, ``boundaries``, ``iterations`` and optionally ``tile_x``),
 validates every item with the rules and messages of ``convolve``, and
-preallocates the outputs and one workspace.  ``run()`` launches one kernel
-that packs every field, then one kernel per pass level over all items
-(rlic_convolve_batch_f32).  ``capture()`` records a run into a CUDA graph so
-that ``replay()`` re-runs the whole batch with a single graph launch; write
-new textures into the plan's input tensors in place between replays.
+preallocates the outputs and one workspace.  ``run()`` makes one persistent
+kernel launch that runs the whole batch from a work queue (pack, traced
+pass and replays of every item, each level of an item waiting for its
+previous one; rlic_convolve_batch_f32), or, with ``per_level=True``, one
+pack launch and one launch per pass level over all items.  ``capture()``
+records a run into a CUDA graph so that ``replay()`` re-runs the whole
+batch with a single graph launch; write new textures into the plan's input
+tensors in place between replays.  ``status()`` reports whether the last
+persistent run's bounded waits all ended.
 
-``autotune_tiles`` picks each item's CTA tile shape by timing the candidates
-on that item, once per distinct (side bucket, kernel length, uv mode).
-Results are bit-identical to one ``convolve`` call per item, whatever the
-tile shapes.
+``autotune_tiles`` picks, per bucket of similar items (side, kernel length,
+uv mode), the CTA tile shape (``tile_x`` x 256 / ``tile_x`` pixels) and the
+tiles per replay work item (``replay_tiles``) by timing the candidates on
+the bucket's first item.  Results are bit-identical to one ``convolve`` call
+per item, whatever the tile shapes.
 """
 
 from __future__ import annotations
@@ -28,6 +33,7 @@ from rlic_gb300 import _native
 from rlic_gb300._lib import _collect_problems, _Ops
 
 TILE_CANDIDATES = (64, 32, 16)
+REPLAY_TILE_CANDIDATES = (2, 4, 8)
 
 
 def _validate_item(k: int, item: dict) -> tuple:
@@ -52,11 +58,12 @@ def _validate_item(k: int, item: dict) -> tuple:
 class BatchPlan:
     """Preallocated batch of convolutions (see the module docstring)."""
 
-    def __init__(self, items: list[dict]) -> None:
+    def __init__(self, items: list[dict], per_level: bool = False) -> None:
         import torch
 
         if not items:
             raise ValueError("empty batch")
+        self.per_level = per_level
         self.lib = _native.lib()
         self.device = items[0]["texture"].device
         self.inputs: list[dict] = []
@@ -75,7 +82,7 @@ class BatchPlan:
                 t["kernel"].data_ptr(), out.data_ptr(), ny, nx, t["kernel"].shape[0],
                 int(item.get("iterations", 1)),
                 _native.UV_MODE_CODES[item.get("uv_mode", "velocity")], xl, xr, yl, yr,
-                int(item.get("tile_x", 0)),
+                int(item.get("tile_x", 0)), int(item.get("replay_tiles", 0)),
             )
         self.items = arr
         self.count = len(items)
@@ -94,10 +101,20 @@ class BatchPlan:
 
         stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         flags = _native.RLIC_FLAG_BATCH_PREPARED if self.prepared else 0
+        if self.per_level:
+            flags |= _native.RLIC_FLAG_BATCH_PER_LEVEL
         _native.check(self.lib.rlic_convolve_batch_f32(
             self.items, self.count, self.workspace.data_ptr(), self.nbytes, stream, flags))
         self.prepared = True
         return self.outputs
+
+    def status(self) -> bool:
+        """True if every bounded wait of the last persistent run ended
+        (synchronises the device)."""
+        rc = self.lib.rlic_batch_status_f32(self.items, self.count, self.workspace.data_ptr())
+        if rc < 0:
+            _native.check(-rc)
+        return rc == 0
 
     def capture(self) -> None:
         """Record one prepared run into a CUDA graph (replay() re-runs it)."""
@@ -128,37 +145,48 @@ def convolve_batch(items: list[dict]) -> list:
 
 def _bucket(item: dict) -> tuple:
     ny, nx = item["texture"].shape
-    return (round(math.log2(max(ny * nx, 1)) / 2), int(item["kernel"].shape[0]),
+    klen = int(item["kernel"].shape[0])
+    return (round(math.log2(max(ny * nx, 1)) / 2), (klen + 15) // 32,
             item.get("uv_mode", "velocity"))
 
 
-def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
-                   repeats: int = 2) -> dict:
-    """Sets item["tile_x"] to the fastest candidate for each distinct bucket.
-
-    Each bucket is timed on its first item as a one-item batch.  Returns the
-    choice per bucket.
-    """
+def _time_plan(plan: "BatchPlan", repeats: int) -> float:
     import torch
 
+    plan.run()
+    torch.cuda.synchronize(plan.device)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(repeats):
+        plan.run()
+    b.record()
+    torch.cuda.synchronize(plan.device)
+    return a.elapsed_time(b) / repeats
+
+
+def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
+                   replay_candidates: tuple = REPLAY_TILE_CANDIDATES,
+                   repeats: int = 2) -> dict:
+    """Sets item["tile_x"] and item["replay_tiles"] to the fastest candidates
+    for each bucket of similar items (side, kernel length in steps of 32 taps,
+    uv mode).
+
+    Each bucket is timed on its first item, as a one-item batch of at most
+    two iterations (a traced pass and a replay): first the tile shapes, then,
+    with the best shape, the tiles per replay work item.  Returns the choice
+    per bucket.
+    """
     choice: dict = {}
     for item in items:
         key = _bucket(item)
         if key not in choice:
-            best, best_ms = candidates[0], float("inf")
-            for tx in candidates:
-                plan = BatchPlan([{**item, "tile_x": tx}])
-                plan.run()
-                torch.cuda.synchronize(plan.device)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record()
-                for _ in range(repeats):
-                    plan.run()
-                b.record()
-                torch.cuda.synchronize(plan.device)
-                ms = a.elapsed_time(b) / repeats
-                if ms < best_ms:
-                    best, best_ms = tx, ms
-            choice[key] = best
-        item["tile_x"] = choice[key]
+            probe = {**item, "iterations": min(int(item.get("iterations", 1)), 2)}
+            best_tx = min(candidates, key=lambda tx: _time_plan(
+                BatchPlan([{**probe, "tile_x": tx}]), repeats))
+            best_rt = 0
+            if probe["iterations"] >= 2:
+                best_rt = min(replay_candidates, key=lambda rt: _time_plan(
+                    BatchPlan([{**probe, "tile_x": best_tx, "replay_tiles": rt}]), repeats))
+            choice[key] = (best_tx, best_rt)
+        item["tile_x"], item["replay_tiles"] = choice[key]
     return choice

@@ -48,16 +48,13 @@ __device__ __forceinline__ int load_level(const BatchLevel& lv, int64_t* starts,
     return m;
 }
 
-__global__ void __launch_bounds__(256)
-batch_pass_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv) {
-    __shared__ int64_t starts[kMaxBatchInSmem];
-    __shared__ int index[kMaxBatchInSmem];
-    __shared__ __align__(16) float wsm[2 * kBatchMaxHalf];
-    const int m = load_level(lv, starts, index);
-    const int64_t tile = blockIdx.x;
-    const int slot = find_instance(starts, m, tile);
-    const BatchInstance& b = insts[index[slot]];
-    const int64_t local = tile - starts[slot];
+// Tile `local` of instance b's traced pass (level 1), by the CTA's 256
+// threads; `wsm` receives the weights (the caller synchronises after).
+// NC: read the field and texture through the read-only cache (they do not
+// change during the launch); false in the persistent kernel, where the pack
+// of the same launch wrote the field.
+template <bool NC>
+__device__ __forceinline__ void trace_tile(const BatchInstance& b, int64_t local, float* wsm) {
     const int klen = b.klen;
     const int kmid = klen / 2;
     const int nf = klen - kmid - 1;
@@ -90,10 +87,10 @@ batch_pass_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv) {
     const bool interior = tile_is_interior(ti, tj, tg, g);
     if (!interior && (i >= b.ny || j >= b.nx)) return;
     // interior tiles of a field without NaN samples skip the per-step NaN test
-    const bool fast = interior && __ldg(b.nan_flag) == 0u;
+    const bool fast = interior && *reinterpret_cast<const volatile unsigned*>(b.nan_flag) == 0u;
     float acc;
 #define RLIC_BATCH_PIXEL(POL, EDGE, MODE, CHECK)                                           \
-    acc = convolve_pixel<float, true, true, POL, EDGE, MODE, int32_t, CHECK>(               \
+    acc = convolve_pixel<float, true, true, POL, EDGE, MODE, int32_t, CHECK, NC>(           \
         i, j, g, uv, src, wsm, wsm + nf_pad, wmid, nf, kmid, b.codes, cl)
     if (b.pol) {
         if (record) {
@@ -120,6 +117,51 @@ batch_pass_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv) {
     level_dst(b, 1)[int64_t(i) * b.nx + j] = acc;
 }
 
+// Loads instance b's step weights and delta table into shared memory (the
+// caller synchronises after).
+__device__ __forceinline__ void replay_setup(const BatchInstance& b, float* wsm, int32_t* table) {
+    const int kmid = b.klen / 2;
+    const int nf = b.klen - kmid - 1;
+    load_step_weights(wsm, b.kernel, b.klen, (nf + 7) & ~7);
+    if (threadIdx.x == 0) fill_delta_table(table, int32_t(b.nx), int32_t(b.ny));
+}
+
+// Tile `local` of instance b's replayed pass at `level` (weights and delta
+// table already in shared memory).
+template <bool NC>
+__device__ __forceinline__ void replay_tile(const BatchInstance& b, int64_t local, int level,
+                                            const float* wsm, const int32_t* table) {
+    const int klen = b.klen;
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nf_pad = (nf + 7) & ~7;
+    const int ti = int(local / b.tiles_x);
+    const int tj = int(local - int64_t(ti) * b.tiles_x);
+    const int tid = threadIdx.x;
+    const int i = ti * b.tile_y + tid / b.tile_x;
+    const int j = tj * b.tile_x + tid % b.tile_x;
+    if (i >= b.ny || j >= b.nx) return;
+    const int64_t npix = int64_t(b.ny) * b.nx;
+    const int p = i * b.nx + j;
+    const float* src = level_src(b, level);
+    float acc = accumulate<float, true>(__ldg(b.kernel + kmid), ld_in<NC>(src + p), 0.f);
+    replay_half<float, true, int32_t, NC>(acc, p, b.codes + p, npix, nf, wsm, table, src);
+    replay_half<float, true, int32_t, NC>(acc, p, b.codes + size_t((nf + 7) / 8) * npix + p,
+                                          npix, kmid, wsm + nf_pad, table, src);
+    level_dst(b, level)[p] = acc;
+}
+
+__global__ void __launch_bounds__(256)
+batch_pass_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv) {
+    __shared__ int64_t starts[kMaxBatchInSmem];
+    __shared__ int index[kMaxBatchInSmem];
+    __shared__ __align__(16) float wsm[2 * kBatchMaxHalf];
+    const int m = load_level(lv, starts, index);
+    const int64_t tile = blockIdx.x;
+    const int slot = find_instance(starts, m, tile);
+    trace_tile<true>(insts[index[slot]], tile - starts[slot], wsm);
+}
+
 __global__ void __launch_bounds__(256)
 batch_gather_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv, int level) {
     __shared__ int64_t starts[kMaxBatchInSmem];
@@ -130,28 +172,112 @@ batch_gather_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv, int 
     const int64_t tile = blockIdx.x;
     const int slot = find_instance(starts, m, tile);
     const BatchInstance& b = insts[index[slot]];
-    const int64_t local = tile - starts[slot];
-    const int klen = b.klen;
-    const int kmid = klen / 2;
-    const int nf = klen - kmid - 1;
-    const int nf_pad = (nf + 7) & ~7;
-    load_step_weights(wsm, b.kernel, klen, nf_pad);
-    if (threadIdx.x == 0) fill_delta_table(table, int32_t(b.nx), int32_t(b.ny));
+    replay_setup(b, wsm, table);
     __syncthreads();
-    const int ti = int(local / b.tiles_x);
-    const int tj = int(local - int64_t(ti) * b.tiles_x);
+    replay_tile<true>(b, tile - starts[slot], level, wsm, table);
+}
+
+// ------------------------------------------------- persistent work queue --
+//
+// One launch runs the whole batch.  Every CTA loops: it takes the next item
+// number from the queue counter (the number for its following item is
+// requested while the current one runs), finds the item's segment, and,
+// unless the segment is a pack, waits until the segment it reads from has
+// finished (thread 0 polls that segment's counter, bounded, then fences).
+// Item numbers are handed out in order and an item only ever waits for items
+// with smaller numbers, each held by a CTA that is already running, so the
+// waits always end; the bound only guards against a fault.  Data written by
+// other CTAs of the launch (the packed field, codes, the previous level's
+// texture) is read with plain coherent loads after the fence, never through
+// the read-only cache.
+
+constexpr int kQueueSegSmem = 2048;          // segment starts kept in shared memory
+constexpr uint32_t kQueueWaitLimit = 1u << 24;  // polls, 128 ns apart
+
+__device__ __forceinline__ int find_segment(const int* starts, int nseg, int item) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (starts[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256)
+batch_queue_kernel(const BatchInstance* __restrict__ insts, BatchQueue q) {
+    __shared__ int seg_start_s[kQueueSegSmem + 1];
+    __shared__ __align__(16) float wsm[2 * kBatchMaxHalf];
+    __shared__ int32_t table[16];
+    __shared__ int cur_item, next_item, cur_seg, stop;
     const int tid = threadIdx.x;
-    const int i = ti * b.tile_y + tid / b.tile_x;
-    const int j = tj * b.tile_x + tid % b.tile_x;
-    if (i >= b.ny || j >= b.nx) return;
-    const int64_t npix = int64_t(b.ny) * b.nx;
-    const int p = i * b.nx + j;
-    const float* src = level_src(b, level);
-    float acc = accumulate<float, true>(__ldg(b.kernel + kmid), __ldg(src + p), 0.f);
-    replay_half<float, true, int32_t>(acc, p, b.codes + p, npix, nf, wsm, table, src);
-    replay_half<float, true, int32_t>(acc, p, b.codes + size_t((nf + 7) / 8) * npix + p, npix,
-                                      kmid, wsm + nf_pad, table, src);
-    level_dst(b, level)[p] = acc;
+    const bool in_smem = q.nseg <= kQueueSegSmem;
+    if (in_smem)
+        for (int k = tid; k <= q.nseg; k += blockDim.x) seg_start_s[k] = q.seg_start[k];
+    if (tid == 0) {
+        next_item = int(atomicAdd(q.next, 1u));
+        stop = 0;
+    }
+    __syncthreads();
+    const int* starts = in_smem ? seg_start_s : q.seg_start;
+    for (;;) {
+        if (tid == 0) {
+            const int item = next_item;
+            cur_item = item;
+            if (item < q.total) {
+                next_item = int(atomicAdd(q.next, 1u));  // in flight while this item runs
+                const int s = find_segment(starts, q.nseg, item);
+                cur_seg = s;
+                const int prev = q.segs[s].prev;
+                if (prev >= 0) {
+                    const unsigned need = unsigned(q.segs[prev].nitems);
+                    const volatile unsigned* d = q.done + prev;
+                    uint32_t polls = 0;
+                    while (*d < need) {
+                        if (++polls > kQueueWaitLimit) {
+                            atomicExch(q.timeout, 1u);
+                            stop = 1;
+                            break;
+                        }
+                        __nanosleep(128);
+                    }
+                    __threadfence();  // acquire: the previous level's writes are visible
+                }
+            }
+        }
+        __syncthreads();
+        if (cur_item >= q.total || stop) break;
+        const BatchSegment seg = q.segs[cur_seg];
+        const int64_t local = cur_item - starts[cur_seg];
+        const BatchInstance& b = insts[seg.inst];
+        if (seg.level == 0) {
+            // pack: pixels [local * chunk, (local + 1) * chunk) of the field
+            const int64_t n = int64_t(b.ny) * b.nx;
+            const int64_t p0 = local * kBatchPackChunk;
+            const int64_t p1 = p0 + kBatchPackChunk < n ? p0 + kBatchPackChunk : n;
+            float2* uv = static_cast<float2*>(b.uv);
+            bool nan = false;
+            for (int64_t k = p0 + tid; k < p1; k += blockDim.x) {
+                const float2 v2 = make_float2(__ldg(b.u + k), __ldg(b.v + k));
+                nan |= isnan(v2.x) || isnan(v2.y);
+                uv[k] = v2;
+            }
+            if (nan) atomicOr(b.nan_flag, 1u);
+        } else if (seg.level == 1) {
+            trace_tile<false>(b, local, wsm);
+        } else {
+            replay_setup(b, wsm, table);
+            __syncthreads();
+            const int64_t t0 = local * b.replay_tiles;
+            const int64_t t1 =
+                t0 + b.replay_tiles < int64_t(b.ntiles) ? t0 + b.replay_tiles : int64_t(b.ntiles);
+            for (int64_t t = t0; t < t1; ++t) replay_tile<false>(b, t, seg.level, wsm, table);
+        }
+        __syncthreads();  // the item's stores (and shared-memory reads) are done
+        if (tid == 0) {
+            __threadfence();  // release the item's stores before counting it
+            atomicAdd(q.done + cur_seg, 1u);
+        }
+    }
 }
 
 // Packs (u, v) of every instance: blockIdx.y selects the instance.
@@ -179,6 +305,17 @@ cudaError_t launch_batch_pack(const BatchInstance* dev, int count, int64_t max_p
     if (bx > 512) bx = 512;
     if (bx < 1) bx = 1;
     batch_pack_kernel<<<dim3(unsigned(bx), unsigned(count)), 256, 0, stream>>>(dev);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_queue(const BatchInstance* dev, const BatchQueue& q,
+                               cudaStream_t stream) {
+    if (q.total <= 0) return cudaSuccess;
+    unsigned grid = 0;
+    cudaError_t e = persistent_grid(batch_queue_kernel, 256, 0, q.total, &grid);
+    if (e != cudaSuccess) return e;
+    batch_queue_kernel<<<grid, 256, 0, stream>>>(dev, q);
     count_launch();
     return cudaGetLastError();
 }

@@ -27,6 +27,7 @@ struct BatchInstance {
     int ny, nx, klen, iterations, pol;
     int bnd[4];
     int tile_x, tile_y, tiles_x, ntiles;
+    int replay_tiles;  // tiles per replay work item of the persistent kernel
 };
 
 // The instances taking part in one pass level, with the first tile of each
@@ -38,8 +39,38 @@ struct BatchLevel {
     int64_t total_tiles;
 };
 
+// The work queue of the persistent batched kernel.  The work of a batch is
+// cut into segments, one per (instance, level): level 0 packs the instance's
+// field in chunks of kBatchPackChunk pixels, level 1 traces it tile by tile,
+// level L >= 2 replays it, replay_tiles tiles per work item.  Segments are
+// ordered level by level (largest instances first within a level) and their
+// items numbered consecutively; CTAs take item numbers from a counter in
+// order, and the items of a segment wait until every item of the segment
+// they read from (the same instance's previous level) has finished.
+constexpr int kBatchPackChunk = 8192;
+
+struct BatchSegment {
+    int inst;     // instance
+    int level;    // 0 pack, 1 traced pass, >= 2 replay
+    int prev;     // segment this one reads (-1: none)
+    int nitems;   // work items
+};
+
+struct BatchQueue {
+    const int* seg_start;           // first item of every segment, nseg + 1 entries
+    const BatchSegment* segs;
+    int nseg;
+    int total;                      // items of the whole batch
+    unsigned* next;                 // next item to take (zeroed before the launch)
+    unsigned* done;                 // finished items per segment (zeroed)
+    unsigned* timeout;              // set when a wait gave up (zeroed)
+};
+
 cudaError_t launch_batch_pack(const BatchInstance* dev, int count, int64_t max_pixels,
                               cudaStream_t stream);
+// One persistent launch that runs the whole queue.
+cudaError_t launch_batch_queue(const BatchInstance* dev, const BatchQueue& q,
+                               cudaStream_t stream);
 cudaError_t launch_batch_level(const BatchInstance* dev, const BatchLevel& lv, int level,
                                cudaStream_t stream);
 

@@ -887,10 +887,22 @@ int kernel_grad_impl(const T* g, const T* x, const void* codes, int64_t ny, int6
 // ------------------------------------------------------------ batched form --
 
 struct BatchLayout {
-    size_t insts, levels, flags, total;
+    size_t insts, levels, flags, queue, counters, total;
     std::vector<size_t> uv, tmp, codes;  // per item
     int max_iterations;
+    int nseg;  // segments of the persistent queue
 };
+
+int batch_replay_tiles(const rlic_batch_item_f32& it) { return it.replay_tiles ? it.replay_tiles : 4; }
+
+// Segments of the persistent queue: one per (item, level) for levels
+// 0 (pack) .. iterations.
+int batch_segments(const rlic_batch_item_f32* items, int count) {
+    int64_t n = 0;
+    for (int k = 0; k < count; ++k)
+        if (items[k].iterations > 0) n += items[k].iterations + 1;
+    return int(n);
+}
 
 bool batch_tile_ok(int tx) { return tx == 8 || tx == 16 || tx == 32 || tx == 64 || tx == 128 || tx == 256; }
 
@@ -910,6 +922,8 @@ int batch_check(const rlic_batch_item_f32* items, int count) {
             return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": iterations must be in [0, 4096]");
         if (it.tile_x != 0 && !batch_tile_ok(it.tile_x))
             return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": tile_x must be 0 or a power of two in [8, 256]");
+        if (it.replay_tiles < 0 || it.replay_tiles > 64)
+            return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": replay_tiles must be in [0, 64]");
         if (!it.texture || !it.u || !it.v || !it.kernel || !it.out)
             return fail(RLIC_ERR_INVALID_ARGUMENT, "item " + std::to_string(k) + ": null array pointer");
     }
@@ -927,6 +941,12 @@ BatchLayout batch_layout(const rlic_batch_item_f32* items, int count) {
     off += align_up(size_t(std::max(L.max_iterations, 1)) * size_t(count) * (sizeof(int64_t) + sizeof(int)));
     L.flags = off;  // one NaN flag per item
     off += align_up(size_t(count) * sizeof(unsigned));
+    L.nseg = batch_segments(items, count);
+    L.queue = off;  // segment starts (nseg + 1 ints), then the segments
+    off += align_up(size_t(L.nseg + 1) * sizeof(int)) +
+           align_up(size_t(L.nseg) * sizeof(rlic::BatchSegment));
+    L.counters = off;  // next item, timeout word, then finished items per segment
+    off += align_up(size_t(L.nseg + 2) * sizeof(unsigned));
     for (int k = 0; k < count; ++k) {
         const auto& it = items[k];
         const size_t n = size_t(it.ny) * size_t(it.nx);
@@ -946,8 +966,9 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
     g_last_error.clear();
     int rc = batch_check(items, count);
     if (rc) return rc;
-    if (flags & ~unsigned(RLIC_FLAG_BATCH_PREPARED))
-        return fail(RLIC_ERR_INVALID_ARGUMENT, "this entry point takes RLIC_FLAG_BATCH_PREPARED only");
+    if (flags & ~unsigned(RLIC_FLAG_BATCH_PREPARED | RLIC_FLAG_BATCH_PER_LEVEL))
+        return fail(RLIC_ERR_INVALID_ARGUMENT,
+                    "this entry point takes RLIC_FLAG_BATCH_PREPARED and RLIC_FLAG_BATCH_PER_LEVEL only");
     if (!workspace) return fail(RLIC_ERR_INVALID_ARGUMENT, "the batched form needs a workspace");
     const BatchLayout L = batch_layout(items, count);
     if (workspace_bytes_ < L.total)
@@ -991,6 +1012,7 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
         b.tile_y = 256 / b.tile_x;
         b.tiles_x = int((it.nx + b.tile_x - 1) / b.tile_x);
         b.ntiles = b.tiles_x * int((it.ny + b.tile_y - 1) / b.tile_y);
+        b.replay_tiles = batch_replay_tiles(it);
         max_pixels = std::max<int64_t>(max_pixels, it.ny * it.nx);
     }
     for (int level = 1; level <= L.max_iterations; ++level) {
@@ -1006,10 +1028,57 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
         }
         levels[level] = rlic::BatchLevel{dev_starts + base, dev_index + base, m, tiles};
     }
+    // the persistent queue: segments level by level, the largest items first
+    // within a level (their previous level was taken first, so it is the
+    // first to be finished)
+    std::vector<int> seg_start(size_t(L.nseg) + 1, 0);
+    std::vector<rlic::BatchSegment> segs(size_t(L.nseg));
+    {
+        std::vector<int> order(count);
+        for (int k = 0; k < count; ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return items[a].ny * items[a].nx > items[b].ny * items[b].nx;
+        });
+        std::vector<int> last(count, -1);  // each item's segment of the previous level
+        int ns = 0;
+        int64_t total = 0;
+        for (int level = 0; level <= L.max_iterations; ++level) {
+            for (int k : order) {
+                const auto& b = insts[k];
+                if (b.iterations < std::max(level, 1)) continue;
+                int64_t nitems;
+                if (level == 0)
+                    nitems = (int64_t(b.ny) * b.nx + rlic::kBatchPackChunk - 1) / rlic::kBatchPackChunk;
+                else if (level == 1)
+                    nitems = b.ntiles;
+                else
+                    nitems = (int64_t(b.ntiles) + b.replay_tiles - 1) / b.replay_tiles;
+                segs[ns] = rlic::BatchSegment{k, level, last[k], int(nitems)};
+                seg_start[ns] = int(total);
+                last[k] = ns;
+                total += nitems;
+                ++ns;
+                if (total > 0x7fffffffLL)
+                    return fail(RLIC_ERR_INVALID_ARGUMENT, "batch too large for one work queue");
+            }
+        }
+        seg_start[ns] = int(total);
+    }
+    auto* dev_seg_start = reinterpret_cast<int*>(ws + L.queue);
+    auto* dev_segs = reinterpret_cast<rlic::BatchSegment*>(
+        ws + L.queue + align_up(size_t(L.nseg + 1) * sizeof(int)));
+    auto* dev_counters = reinterpret_cast<unsigned*>(ws + L.counters);
     if (!(flags & RLIC_FLAG_BATCH_PREPARED)) {
         // pageable copies: the call returns once the host tables are staged
         RLIC_CUDA_TRY(cudaMemcpyAsync(dev_insts, insts.data(), insts.size() * sizeof(insts[0]),
                                       cudaMemcpyHostToDevice, stream));
+        RLIC_CUDA_TRY(cudaMemcpyAsync(dev_seg_start, seg_start.data(),
+                                      seg_start.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                      stream));
+        if (!segs.empty())
+            RLIC_CUDA_TRY(cudaMemcpyAsync(dev_segs, segs.data(),
+                                          segs.size() * sizeof(rlic::BatchSegment),
+                                          cudaMemcpyHostToDevice, stream));
         RLIC_CUDA_TRY(cudaMemcpyAsync(dev_starts, starts.data(), starts.size() * sizeof(int64_t),
                                       cudaMemcpyHostToDevice, stream));
         RLIC_CUDA_TRY(cudaMemcpyAsync(dev_index, index.data(), index.size() * sizeof(int),
@@ -1022,10 +1091,39 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
                                           size_t(items[k].ny) * size_t(items[k].nx) * 4, stream));
     if (L.max_iterations == 0) return RLIC_OK;
     RLIC_CUDA_TRY(cudaMemsetAsync(ws + L.flags, 0, size_t(count) * sizeof(unsigned), stream));
-    RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
-    for (int level = 1; level <= L.max_iterations; ++level)
-        RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));
+    if (flags & RLIC_FLAG_BATCH_PER_LEVEL) {
+        RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
+        for (int level = 1; level <= L.max_iterations; ++level)
+            RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));
+        return RLIC_OK;
+    }
+    RLIC_CUDA_TRY(cudaMemsetAsync(dev_counters, 0, size_t(L.nseg + 2) * sizeof(unsigned), stream));
+    rlic::BatchQueue q;
+    q.seg_start = dev_seg_start;
+    q.segs = dev_segs;
+    q.nseg = L.nseg;
+    q.total = seg_start[L.nseg];
+    q.next = dev_counters;
+    q.timeout = dev_counters + 1;
+    q.done = dev_counters + 2;
+    RLIC_CUDA_TRY(rlic::launch_batch_queue(dev_insts, q, stream));
     return RLIC_OK;
+}
+
+// 1 if a persistent batched run of these items on this workspace gave up a
+// wait, 0 if not (synchronises the device).
+int batch_status_f32(const rlic_batch_item_f32* items, int count, const void* workspace) {
+    g_last_error.clear();
+    int rc = batch_check(items, count);
+    if (rc) return -rc;
+    if (!workspace) return -fail(RLIC_ERR_INVALID_ARGUMENT, "null workspace");
+    const BatchLayout L = batch_layout(items, count);
+    unsigned v = 0;
+    const cudaError_t e = cudaMemcpy(&v, static_cast<const unsigned char*>(workspace) +
+                                             L.counters + sizeof(unsigned),
+                                     sizeof(v), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return -cuda_fail(e, "cudaMemcpy");
+    return v ? 1 : 0;
 }
 
 // ------------------------------------------------------- no-allocation path --
@@ -1342,6 +1440,10 @@ size_t rlic_batch_workspace_bytes_f32(const rlic_batch_item_f32* items, int coun
 int rlic_convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* workspace,
                             size_t workspace_bytes, void* stream, unsigned flags) {
     return convolve_batch_f32(items, count, workspace, workspace_bytes, stream, flags);
+}
+
+int rlic_batch_status_f32(const rlic_batch_item_f32* items, int count, const void* workspace) {
+    return batch_status_f32(items, count, workspace);
 }
 
 int rlic_convolve_f32_noalloc(const float* texture, const float* u, const float* v,

@@ -632,6 +632,19 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
     }
 }
 
+// A load of kernel input: through the read-only data cache (NC, the
+// default: the data does not change while the kernel runs), or a plain
+// coherent load, for data that other CTAs of the same launch wrote before
+// an acquire (the persistent batched kernel).
+template <bool NC, typename V>
+__device__ __forceinline__ V ld_in(const V* p) {
+    if constexpr (NC) {
+        return __ldg(p);
+    } else {
+        return *p;
+    }
+}
+
 // Per-trace state of convole_single_pixel (src/lib.rs:314-323).
 template <typename T, typename I>
 struct TraceState {
@@ -648,12 +661,12 @@ struct TraceState {
 // backward trace, advance, then accumulate weight * texture at the new cell.
 // `code` receives the step code.
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
-          bool SAMPLE, typename I, bool NAN_CHECK = true>
+          bool SAMPLE, typename I, bool NAN_CHECK = true, bool NC = true>
 __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
                                            const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
                                            const T* __restrict__ tex, uint32_t& code) {
-    const auto p = __ldg(uv + st.cell);
+    const auto p = ld_in<NC>(uv + st.cell);
     T pu = p.x, pv = p.y;
     // (NAN_CHECK false: the caller knows the field holds no NaN sample)
     if (NAN_CHECK && (is_nan(pu) || is_nan(pv))) return false;
@@ -678,7 +691,7 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
     }
     code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, st.last,
                                              g);
-    if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, __ldg(tex + st.cell), acc);
+    if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, ld_in<NC>(tex + st.cell), acc);
     return true;
 }
 
@@ -692,7 +705,7 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
 // RECORD the word is stored at words[group * stride].  A trace that stops on
 // NaN stores the stop code in place of its step and nothing after it.
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
-          bool SAMPLE, bool RECORD, typename I, bool NAN_CHECK = true>
+          bool SAMPLE, bool RECORD, typename I, bool NAN_CHECK = true, bool NC = true>
 __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
                                            const T* __restrict__ tex, const T* w, int count,
@@ -713,7 +726,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK, NC>(
                     st, acc, SAMPLE ? wq[b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                 return;
@@ -727,7 +740,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
         uint32_t word = 0;
         for (int b = 0; b < rest; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK, NC>(
                     st, acc, SAMPLE ? w[8 * full + b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(full) * stride] = word | (kStop << (4 * b));
                 return;

@@ -132,7 +132,7 @@ struct CodeLayout {
 enum PassMode : int { kSample = 0, kSampleRecord = 1, kRecordOnly = 2 };
 
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, int MODE, typename I,
-          bool NAN_CHECK = true>
+          bool NAN_CHECK = true, bool NC = true>
 __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
                                             const typename Vec2<T>::type* __restrict__ uv,
                                             const T* __restrict__ tex, const T* wf, const T* wb,
@@ -142,12 +142,12 @@ __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
     constexpr bool RECORD = MODE != kSample;
     const I p = i * g.nx + j;
     T acc = T(0);
-    if constexpr (SAMPLE) acc = accumulate<T, FMA>(wmid, __ldg(tex + p), T(0));
+    if constexpr (SAMPLE) acc = accumulate<T, FMA>(wmid, ld_in<NC>(tex + p), T(0));
     uint32_t* words_f = RECORD ? codes + p : nullptr;
     uint32_t* words_b = RECORD ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : nullptr;
-    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD, I, NAN_CHECK>(
+    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
         acc, i, j, g, uv, tex, wf, nf, words_f, cl.npix);
-    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD, I, NAN_CHECK>(
+    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
         acc, i, j, g, uv, tex, wb, kmid, words_b, cl.npix);
     return acc;
 }
@@ -202,17 +202,17 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
 // word q+1 are in flight while the 8 ordered FMAs of word q run, so the
 // accumulation order (that of the traced pass) is kept while the load
 // latency is hidden.
-template <typename T, typename I>
+template <typename T, typename I, bool NC = true>
 __device__ __forceinline__ void gather8(I& cell, uint32_t wd, const I* table,
                                         const T* __restrict__ tex, T x[8]) {
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         cell += table[(wd >> (4 * b)) & 15u];
-        x[b] = __ldg(tex + cell);
+        x[b] = ld_in<NC>(tex + cell);
     }
 }
 
-template <typename T, bool FMA, typename I>
+template <typename T, bool FMA, typename I, bool NC = true>
 __device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restrict__ words,
                                             int64_t npix, int count, const T* w, const I* table,
                                             const T* __restrict__ tex) {
@@ -221,15 +221,15 @@ __device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restr
     int q = 0;
     // pipelined run of full words without stop codes
     if (full > 0) {
-        uint32_t wd = __ldg(words);
+        uint32_t wd = ld_in<NC>(words);
         if (!word_has_stop(wd)) {
             T x[8];
-            gather8<T, I>(cell, wd, table, tex, x);
+            gather8<T, I, NC>(cell, wd, table, tex, x);
             for (q = 1; q < full; ++q) {
-                wd = __ldg(words + size_t(q) * size_t(npix));
+                wd = ld_in<NC>(words + size_t(q) * size_t(npix));
                 if (word_has_stop(wd)) break;
                 T y[8];
-                gather8<T, I>(cell, wd, table, tex, y);
+                gather8<T, I, NC>(cell, wd, table, tex, y);
                 const T* wq = w + 8 * (q - 1);
 #pragma unroll
                 for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
@@ -245,13 +245,13 @@ __device__ __forceinline__ void replay_half(T& acc, I p, const uint32_t* __restr
     for (; q <= full; ++q) {
         const int n = (q < full) ? 8 : (count & 7);
         if (n == 0) break;
-        const uint32_t wd = __ldg(words + size_t(q) * size_t(npix));
+        const uint32_t wd = ld_in<NC>(words + size_t(q) * size_t(npix));
         const T* wq = w + 8 * q;
         for (int b = 0; b < n; ++b) {
             const uint32_t code = (wd >> (4 * b)) & 15u;
             if (code == kStop) return;
             cell += table[code];
-            acc = accumulate<T, FMA>(wq[b], __ldg(tex + cell), acc);
+            acc = accumulate<T, FMA>(wq[b], ld_in<NC>(tex + cell), acc);
         }
     }
 }

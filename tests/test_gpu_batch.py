@@ -1,6 +1,7 @@
 """Batched form: one call for many instances of uneven sizes, kernels,
 boundaries, uv modes and iteration counts, bit-identical to one convolve
-call per instance, also when replayed from a captured CUDA graph."""
+call per instance, also when replayed from a captured CUDA graph, both in
+one persistent launch from a work queue and with one launch per level."""
 
 from __future__ import annotations
 
@@ -43,25 +44,48 @@ def _mixed_items():
     return items
 
 
-def test_batch_matches_individual_calls() -> None:
+@pytest.mark.parametrize("per_level", [False, True], ids=["queue", "per-level"])
+def test_batch_matches_individual_calls(per_level) -> None:
     import torch
 
     items = _mixed_items()
-    outs = convolve_batch(items)
+    for k, it in enumerate(items):
+        it["replay_tiles"] = [0, 1, 3, 64][k % 4]
+    plan = BatchPlan(items, per_level=per_level)
+    outs = plan.run()
     for it, got, want in zip(items, outs, _reference(items)):
         if it["iterations"] == 0:
             assert not got.any()
             continue
         assert torch.equal(got.view(torch.int32), want.view(torch.int32))
+    assert plan.status()
 
 
-def test_batch_graph_replay_with_new_textures() -> None:
+def test_batch_queue_many_small_instances() -> None:
+    """300 instances of 16-96 pixels a side in one queue: thousands of
+    segments (beyond the 2048 the kernel keeps in shared memory), so the
+    segment search runs in global memory; every level waits for its
+    previous one."""
+    import torch
+
+    items = batch_case(count=300, seed=13, min_side=16, max_side=96)
+    for it in items:
+        it["iterations"] = 10
+    plan = BatchPlan(items)
+    outs = plan.run()
+    for got, want in zip(outs, _reference(items)):
+        assert torch.equal(got.view(torch.int32), want.view(torch.int32))
+    assert plan.status()
+
+
+@pytest.mark.parametrize("per_level", [False, True], ids=["queue", "per-level"])
+def test_batch_graph_replay_with_new_textures(per_level) -> None:
     import torch
 
     items = _mixed_items()
     for it in items:
         it["iterations"] = max(it["iterations"], 1)
-    plan = BatchPlan(items)
+    plan = BatchPlan(items, per_level=per_level)
     plan.capture()
     for round_ in range(2):
         gen = torch.Generator(device="cuda").manual_seed(round_)
@@ -76,8 +100,11 @@ def test_batch_graph_replay_with_new_textures() -> None:
 
 def test_autotune_sets_tiles() -> None:
     items = batch_case(count=3, seed=5, min_side=64, max_side=200)
+    for it in items:
+        it["iterations"] = 3
     choice = autotune_tiles(items, repeats=1)
     assert choice and all(it["tile_x"] in (64, 32, 16) for it in items)
+    assert all(it["replay_tiles"] in (2, 4, 8) for it in items)
 
 
 def test_batch_validates_items() -> None:
