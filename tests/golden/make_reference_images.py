@@ -13,7 +13,7 @@ This script decodes the two PNG files (zlib and the five PNG row filters,
 no imaging library needed), cuts out the drawing area of every LIC panel
 inside its frame lines, and stores its green channel (viridis' green rises
 monotonically with the mapped value, so it orders pixels as the results
-do) in ``reference_images.npz``:
+do) in ``figures/reference_images.npz``:
 
   base_n1, base_n5, base_n100   README example, 1, 5 and 100 iterations
   pol_velocity, pol_polarization  polarization example, both uv modes
@@ -100,7 +100,7 @@ def main(reference: Path) -> None:
     base = panels(read_png(reference / "static" / "base_example_out.png"))
     pol = panels(read_png(reference / "static" / "polarization_example.png"))
     np.savez_compressed(
-        HERE / "reference_images.npz",
+        HERE / "figures" / "reference_images.npz",
         base_n1=base[0], base_n5=base[1], base_n100=base[2],
         pol_velocity=pol[1], pol_polarization=pol[2],
         frame=np.array([FRAME], dtype=np.int64),

@@ -4,7 +4,7 @@ The reference's Rust core cannot run here, but its repository ships the
 figures of its README, drawn from results of that core: the README example
 after 1, 5 and 100 iterations (``static/base_example_out.png``) and the
 polarization example in both uv modes (``static/polarization_example.png``).
-``tests/golden/reference_images.npz`` holds their LIC panels (made by
+``tests/golden/figures/reference_images.npz`` holds their LIC panels (made by
 ``tests/golden/make_reference_images.py``): 340 x 340 pixels of viridis'
 green channel, which rises monotonically with the mapped value.
 
@@ -28,7 +28,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_images.npz"
+GOLDEN = Path(__file__).resolve().parent / "golden" / "figures" / "reference_images.npz"
 MATCH = 0.998  # rank correlation of a result with its own panel
 
 

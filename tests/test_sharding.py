@@ -105,3 +105,23 @@ def test_sharded_equals_full_image(tmp_path, oracle, world, ny, nx, klen, bounda
         z = np.load(tmp_path / f"rank{r}.npz")
         got[int(z["r0"]):int(z["r1"])] = z["rows"]
     np.testing.assert_array_equal(got, want)
+
+
+def test_single_rank_band_wraps_onto_itself(oracle) -> None:
+    """One rank, periodic y: the extended band holds copies of the rank's own
+    rows at both ends (no process group is needed), over 3 passes."""
+    from rlic_gb300.sharding import convolve_row_sharded
+
+    tex, u, v, k = _case(20, 24, 9, seed=7)
+
+    def compute(tex_ext, u_ext, v_ext, kernel, mode, spec):
+        return oracle.convolve(tex_ext, u_ext, v_ext, kernel, uv_mode=mode, boundaries=spec,
+                               iterations=1)
+
+    r0, r1, rows = convolve_row_sharded(tex, u, v, kernel=k, uv_mode="polarization",
+                                        boundaries="periodic", iterations=3, rank=0, world=1,
+                                        compute=compute)
+    want = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries="periodic",
+                           iterations=3)
+    assert (r0, r1) == (0, 20)
+    np.testing.assert_array_equal(rows, want)
