@@ -68,6 +68,8 @@ def parse_args() -> argparse.Namespace:
                    help="target CPU time of the oracle baseline sample")
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--shard", action="store_true",
+                   help="strong scaling: split one image into row bands across the ranks")
     p.add_argument("--replay", choices=["auto", "l1", "staged"], default="auto",
                    help="how replayed passes gather: the library's default, through L1, or "
                         "from TMA-staged shared-memory boxes")
@@ -886,6 +888,70 @@ def run_batched(args) -> None:
     }), flush=True)
 
 
+def run_shard(args, dist: Dist) -> None:
+    """Strong scaling of one image: the 8192^2 workload split into row bands,
+    one per rank (rlic_gb300.sharding), each band device-resident with its
+    own path cache, halo rows exchanged over NCCL between passes.  value =
+    the image's samples per second over the slowest rank."""
+    import torch
+
+    from rlic_gb300.sharding import GpuBandEngine, HaloExchange, ShardPlan
+    from rlic_gb300.workloads import fourier_vortex_case
+
+    dist.init("nccl")
+    dev = torch.device("cuda", dist.local_rank)
+    torch.cuda.set_device(dev)
+    n = args.size
+    case = fourier_vortex_case(n=n, device="cpu")
+    plan = ShardPlan(n, dist.world, KLEN // 2, periodic_y=False)
+    spec = plan.local_boundaries({"x": ("periodic", "periodic"), "y": ("closed", "closed")})
+    rows = plan.ext_rows[dist.rank]
+    off = plan.owned_offset[dist.rank]
+    r0, r1 = plan.bands[dist.rank]
+    eng = GpuBandEngine(case["u"][rows], case["v"][rows], case["kernel"], "polarization", spec,
+                        ITERS, device=dev)
+    halo = HaloExchange(plan, dist.rank)
+    tex0 = torch.from_numpy(np.ascontiguousarray(case["texture"][rows])).to(dev)
+    bufs = [torch.empty_like(tex0) for _ in range(2)]
+
+    def step():
+        t = tex0
+        for it in range(ITERS):
+            out = eng.first(t) if it == 0 else eng.next(t)
+            if it + 1 < ITERS:
+                t = bufs[it % 2]
+                halo.fill(out[off:off + (r1 - r0)], t)
+        return out
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    ms = dist.max(ev0.elapsed_time(ev1), dev) / args.steps
+    samples = n * n * KLEN * ITERS
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": samples / (ms / 1e3) / 1e9, "unit": UNIT,
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Fourier modes + point vortices, 1% zero cells)",
+            "config": {**config(n, args.replay),
+                       "sharding": f"{dist.world} row bands with a {KLEN // 2}-row halo, "
+                                   "halo rows exchanged between passes"},
+        }), flush=True)
+    dist.close()
+
+
 def main() -> None:
     args = parse_args()
     dist = Dist()
@@ -902,6 +968,8 @@ def main() -> None:
         run_equalize(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.shard:
+        run_shard(args, dist)
     else:
         run_gb300(args, dist)
 
