@@ -84,9 +84,11 @@ RLIC_API const char *rlic_last_error(void);
  * Device scratch, in bytes, that rlic_convolve_f32/_f64 need for an image of
  * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps,
  * `iterations` passes and the given flags: the packed (u, v) field, for two
- * or more iterations one ping-pong texture buffer and (unless
- * RLIC_FLAG_NO_PATH_CACHE) the path cache, a copy of the kernel and a
- * flag that records whether the field holds a NaN sample.
+ * or more iterations one ping-pong texture buffer, (unless
+ * RLIC_FLAG_NO_PATH_CACHE) the path cache for two or more iterations or for
+ * an image small enough to trace as split halves (rlic_set_split_pixels), a
+ * copy of the kernel and a flag that records whether the field holds a NaN
+ * sample.
  * 0 on invalid arguments.
  */
 RLIC_API size_t rlic_workspace_bytes(int64_t ny, int64_t nx, int64_t klen, int64_t iterations,
@@ -418,6 +420,19 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
 #define RLIC_REPLAY_L1 1
 #define RLIC_REPLAY_STAGED 2
 RLIC_API int rlic_set_replay_mode(int mode, int stage_rows);
+/*
+ * Images of at most max_pixels pixels (default 524288 = 2^19) trace their
+ * first pass as split halves, one thread per half-streamline, recording the
+ * path cache, and then replay it: on images too small to fill the GPU this
+ * doubles the parallelism of the streamline arithmetic.  Bit-identical to
+ * the single traced pass; 0 turns it off.  The workspace of such calls
+ * holds the path cache even for one iteration (rlic_workspace_bytes counts
+ * it under the setting in force), so change the setting only between calls
+ * that size their workspace again.  RLIC_FLAG_NO_PATH_CACHE calls never
+ * split.  Affects calls made after it on any thread.  No counterpart in the
+ * reference (a tuning knob of this implementation).
+ */
+RLIC_API int rlic_set_split_pixels(int64_t max_pixels);
 /*
  * 1 if a staged replay ever gave up waiting for one of its copies (each wait
  * is bounded; the CTA then returns and its remaining pixels are not written),

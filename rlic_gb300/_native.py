@@ -103,6 +103,7 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_equalize_histogram_f64": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),
     "rlic_set_replay_mode": ([_INT, _INT], _INT),
+    "rlic_set_split_pixels": ([_I64], _INT),
     "rlic_stage_timeouts": ([], _INT),
     "rlic_kernel_launch_count": ([], ctypes.c_uint64),
     "rlic_release_cached_memory": ([], _INT),
@@ -201,6 +202,11 @@ def launch_count() -> int:
 
 def set_block_shape(block_x: int, block_y: int) -> None:
     check(lib().rlic_set_block_shape(block_x, block_y))
+
+
+def set_split_pixels(max_pixels: int) -> None:
+    """Images of at most max_pixels trace their first pass as split halves."""
+    check(lib().rlic_set_split_pixels(max_pixels))
 
 
 def set_replay_mode(mode: int, stage_rows: int = 0) -> None:

@@ -191,6 +191,13 @@ batch_gather_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv, int 
 // texture) is read with plain coherent loads after the fence, never through
 // the read-only cache.
 
+// Minimum resident CTAs per SM requested from the register allocator for
+// the persistent kernel (its registers are those of its costliest path, the
+// traced pass; the replays run at the same occupancy).
+#ifndef RLIC_BATCH_QUEUE_MIN_BLOCKS
+#define RLIC_BATCH_QUEUE_MIN_BLOCKS 1
+#endif
+
 constexpr int kQueueSegSmem = 2048;          // segment starts kept in shared memory
 constexpr uint32_t kQueueWaitLimit = 1u << 24;  // polls, 128 ns apart
 
@@ -203,7 +210,7 @@ __device__ __forceinline__ int find_segment(const int* starts, int nseg, int ite
     return lo;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, RLIC_BATCH_QUEUE_MIN_BLOCKS)
 batch_queue_kernel(const BatchInstance* __restrict__ insts, BatchQueue q) {
     __shared__ int seg_start_s[kQueueSegSmem + 1];
     __shared__ __align__(16) float wsm[2 * kBatchMaxHalf];

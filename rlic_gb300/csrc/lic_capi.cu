@@ -162,6 +162,10 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 #define RLIC_HOST_CHUNKS 8
 #endif
 
+#ifndef RLIC_SPLIT_PIXELS_DEFAULT
+#define RLIC_SPLIT_PIXELS_DEFAULT (1 << 19)
+#endif
+
 // A non-blocking stream per device for the uploads of host-memory calls, at
 // the greatest priority: the block scheduler then gives the upload kernels
 // the SM slots that the traced pass's blocks free, instead of queueing them
@@ -274,6 +278,18 @@ Shape make_shape(int64_t ny, int64_t nx, const int bnd[4]) {
     return sh;
 }
 
+// Images of at most this many pixels trace their first pass as split
+// halves (lic_record_halves_kernel, one thread per half-streamline) followed
+// by a replay: their tiles alone cannot fill the GPU, and the split doubles
+// the parallelism of the streamline arithmetic (rlic_set_split_pixels).
+std::atomic<int64_t> g_split_pixels{RLIC_SPLIT_PIXELS_DEFAULT};
+
+int64_t split_pixels() { return g_split_pixels.load(); }
+
+bool use_split(int64_t ny, int64_t nx, int64_t klen, unsigned flags) {
+    return klen > 1 && !(flags & RLIC_FLAG_NO_PATH_CACHE) && ny * nx <= split_pixels();
+}
+
 bool use_path_cache(int64_t iterations, int64_t klen, unsigned flags) {
     return iterations >= 2 && klen > 1 && !(flags & RLIC_FLAG_NO_PATH_CACHE);
 }
@@ -296,7 +312,8 @@ WorkspaceLayout workspace_layout(int64_t ny, int64_t nx, int64_t klen, int64_t i
     w.tmp = off;
     if (iterations >= 2) off += align_up(n * s);
     w.codes = off;
-    if (use_path_cache(iterations, klen, flags)) off += align_up(code_bytes(ny, nx, klen));
+    if (use_path_cache(iterations, klen, flags) || use_split(ny, nx, klen, flags))
+        off += align_up(code_bytes(ny, nx, klen));
     w.kernel = off;
     off += align_up(size_t(klen) * s);
     w.nan = off;  // flag: the packed field holds a NaN sample
@@ -329,7 +346,8 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     void* uv = ws + wl.uv;
     T* tmp = reinterpret_cast<T*>(ws + wl.tmp);
     uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
-    const bool cache = use_path_cache(iterations, klen, flags);
+    const bool split = use_split(ny, nx, klen, flags);
+    const bool cache = use_path_cache(iterations, klen, flags) || split;
     const Shape sh = make_shape(ny, nx, bnd);
     LaunchConfig lc = launch_config();
     if (!uv_ready) {
@@ -345,7 +363,12 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
             before_last();
             if (final_out) dst = final_out;
         }
-        if (it == 0 || !cache) {
+        if (it == 0 && split) {
+            RLIC_CUDA_TRY(rlic::launch_record_halves(var, texture, uv, int(klen), sh, lc, codes,
+                                                     stream));
+            RLIC_CUDA_TRY(replay_pass(var.fma, src, codes, kernel, int(klen), sh, lc, dst,
+                                      stream));
+        } else if (it == 0 || !cache) {
             RLIC_CUDA_TRY(rlic::launch_pass(var, cache ? rlic::kPassSampleRecord : rlic::kPassSample,
                                             src, uv, kernel, int(klen), sh, lc, dst, codes,
                                             stream));
@@ -485,7 +508,10 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
         RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
         unsigned char* uvb = ws + wl.uv;
-        const bool cache = use_path_cache(iterations, klen, flags);
+        // small images (one upload chunk) trace their first pass as split
+        // halves, then replay it
+        const bool split = use_split(ny, nx, klen, flags) && nchunks == 1;
+        const bool cache = use_path_cache(iterations, klen, flags) || split;
         const Shape sh = make_shape(ny, nx, bnd);
         const LaunchConfig lc = launch_config();
         const int64_t tiles_x = (nx + lc.block_x - 1) / lc.block_x;
@@ -558,8 +584,15 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 // a NaN in a chunk that has not arrived yet cannot be reached
                 // from these tile rows, so the flag's value now suffices
                 part.field_nan = nan_flag;
-                RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen), sh,
-                                                part, dst_of(0), codes, stream));
+                if (split) {
+                    RLIC_CUDA_TRY(rlic::launch_record_halves(var, d_tex, uvb, int(klen), sh, part,
+                                                             codes, stream));
+                    RLIC_CUDA_TRY(replay_pass(var.fma, d_tex, codes, d_kernel, int(klen), sh,
+                                              part, dst_of(0), stream));
+                } else {
+                    RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen),
+                                                    sh, part, dst_of(0), codes, stream));
+                }
                 tr = tr_end;
             }
         }
@@ -1462,6 +1495,13 @@ int rlic_set_replay_mode(int mode, int stage_rows) {
         return fail(RLIC_ERR_INVALID_ARGUMENT, "stage_rows must be 0 or a multiple of 4 in [4, 64]");
     g_replay_mode.store(mode);
     rlic::set_stage_rows(stage_rows ? stage_rows : 24);
+    return RLIC_OK;
+}
+
+int rlic_set_split_pixels(int64_t max_pixels) {
+    g_last_error.clear();
+    if (max_pixels < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "max_pixels must be >= 0");
+    g_split_pixels.store(max_pixels);
     return RLIC_OK;
 }
 

@@ -196,6 +196,49 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
     if constexpr (MODE != kRecordOnly) tex_out[i * g.nx + j] = acc;
 }
 
+// Records the step codes of one half of every pixel's streamline, without
+// sampling: CTA 2 t traces the forward halves of tile t, CTA 2 t + 1 the
+// backward halves.  On images too small to fill the GPU, splitting the two
+// halves over two threads doubles the parallelism of the streamline
+// arithmetic (the trace's work is a serial chain per half); a replay then
+// accumulates every pixel in the reference's order (centre, forward taps
+// ascending, backward taps descending), so the output is the traced pass's.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, typename I>
+__global__ void __launch_bounds__(256, (PassMinBlocks<T, I>::value))
+lic_record_halves_kernel(const typename Vec2<T>::type* __restrict__ uv, int klen, Geometry<I> g,
+                         TileGrid<I> tg, uint32_t* __restrict__ codes, CodeLayout cl,
+                         const unsigned* __restrict__ field_nan) {
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const I tile = tg.tile_base + I(blockIdx.x >> 1);
+    const bool backward = (blockIdx.x & 1u) != 0;
+    const I ti = tile / tg.tiles_x;
+    const I tj = tile - ti * tg.tiles_x;
+    const I i = ti * tg.by + I(threadIdx.y);
+    const I j = tj * tg.bx + I(threadIdx.x);
+    const bool interior = tile_is_interior(ti, tj, tg, g);
+    if (!interior && (i >= g.ny || j >= g.nx)) return;
+    const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
+    const I p = i * g.nx + j;
+    uint32_t* words = backward ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : codes + p;
+    const int count = backward ? kmid : nf;
+    T acc = T(0);
+#define RLIC_HALF(BACK, EDGE, CHECK)                                                        \
+    trace_half<T, FMA, BRANCHLESS, POL, BACK, EDGE, false, true, I, CHECK>(                  \
+        acc, i, j, g, uv, static_cast<const T*>(nullptr), static_cast<const T*>(nullptr),  \
+        count, words, cl.npix)
+    if (backward) {
+        if (interior && nan_free) RLIC_HALF(true, false, false);
+        else if (interior) RLIC_HALF(true, false, true);
+        else RLIC_HALF(true, true, true);
+    } else {
+        if (interior && nan_free) RLIC_HALF(false, false, false);
+        else if (interior) RLIC_HALF(false, false, true);
+        else RLIC_HALF(false, true, true);
+    }
+#undef RLIC_HALF
+}
+
 // Replays `count` recorded steps of one half from pixel p.  A word holds 8
 // steps.  Words without a stop code (all of them unless the field holds
 // NaNs) are gathered branch-free, and one word ahead: the 8 texture loads of
@@ -800,6 +843,42 @@ cudaError_t launch_pass_i(const Variant& var, int mode, const T* tex_in, const v
     return cudaErrorInvalidValue;
 }
 
+template <typename T>
+cudaError_t launch_record_halves_t(const Variant& var, const void* uv, int klen, const Shape& sh,
+                                   const LaunchConfig& lc, uint32_t* codes,
+                                   cudaStream_t stream) {
+    if (!sh.small_index()) return cudaErrorInvalidValue;
+    const auto g = make_geometry<int32_t>(sh);
+    const auto tg = make_tiles<int32_t>(sh, lc, klen);
+    const auto cl = make_code_layout(sh, klen);
+    const int64_t count = lc.tile_count ? lc.tile_count : int64_t(tg.ntiles) - lc.tile_begin;
+    if (count <= 0) return cudaSuccess;
+    if (2 * count > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const auto* p = static_cast<const typename Vec2<T>::type*>(uv);
+    const dim3 grid(unsigned(2 * count)), block(lc.block_x, lc.block_y);
+    const int code = (var.fma ? 4 : 0) | (var.branchless ? 2 : 0) | (var.pol ? 1 : 0);
+#define RLIC_HALVES_CASE(C, F, B, P)                                                         \
+    case C:                                                                                  \
+        lic_record_halves_kernel<T, F, B, P, int32_t><<<grid, block, 0, stream>>>(           \
+            p, klen, g, tg, codes, cl, lc.field_nan);                                        \
+        break;
+    switch (code) {
+        RLIC_HALVES_CASE(0, false, false, false)
+        RLIC_HALVES_CASE(1, false, false, true)
+        RLIC_HALVES_CASE(2, false, true, false)
+        RLIC_HALVES_CASE(3, false, true, true)
+        RLIC_HALVES_CASE(4, true, false, false)
+        RLIC_HALVES_CASE(5, true, false, true)
+        RLIC_HALVES_CASE(6, true, true, false)
+        RLIC_HALVES_CASE(7, true, true, true)
+        default:
+            return cudaErrorInvalidValue;
+    }
+#undef RLIC_HALVES_CASE
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <typename T, bool FMA, typename I>
 cudaError_t launch_gather_t(const T* tex_in, const uint32_t* codes, const T* kernel, int klen,
                             const Shape& sh, const LaunchConfig& lc, T* tex_out,
@@ -996,6 +1075,12 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
                                                        tex_out, stream)                      \
                    : launch_gather_t<T, false, int64_t>(tex_in, codes, kernel, klen, sh, lc, \
                                                         tex_out, stream);                    \
+    }                                                                                        \
+    cudaError_t launch_record_halves(const Variant& var, const T* /*type tag*/,              \
+                                     const void* uv, int klen, const Shape& sh,              \
+                                     const LaunchConfig& lc, uint32_t* codes,                \
+                                     cudaStream_t stream) {                                  \
+        return launch_record_halves_t<T>(var, uv, klen, sh, lc, codes, stream);              \
     }                                                                                        \
     cudaError_t launch_trace_cells(const Variant& var, const T* /*type tag*/, const void* uv, \
                                    const Shape& sh, int klen, int64_t npix,                  \

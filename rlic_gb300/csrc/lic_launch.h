@@ -74,6 +74,9 @@ inline int64_t code_words_per_pixel(int64_t klen) {
     cudaError_t launch_gather(bool fma, const T* tex_in, const uint32_t* codes,            \
                               const T* kernel, int klen, const Shape& sh,                  \
                               const LaunchConfig& lc, T* tex_out, cudaStream_t stream);    \
+    cudaError_t launch_record_halves(const Variant& var, const T* type_tag, const void* uv, \
+                                     int klen, const Shape& sh, const LaunchConfig& lc,    \
+                                     uint32_t* codes, cudaStream_t stream);                \
     cudaError_t launch_trace_cells(const Variant& var, const T* type_tag, const void* uv,  \
                                    const Shape& sh, int klen, int64_t npix,                \
                                    const int64_t* pix, int64_t* cells, cudaStream_t stream); \
