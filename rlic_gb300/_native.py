@@ -36,7 +36,7 @@ RLIC_FLAG_NO_BRANCHLESS = 0x4
 RLIC_FLAG_NO_PATH_CACHE = 0x8
 RLIC_FLAG_CHECK_TEXTURE = 0x20
 RLIC_FLAG_FIELD_NAN_FREE = 0x40
-RLIC_FLAG_BATCH_PER_LEVEL = 0x80
+RLIC_FLAG_BATCH_QUEUE = 0x80
 
 RLIC_STORAGE_FP16 = 0
 RLIC_STORAGE_BF16 = 1

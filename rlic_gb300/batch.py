@@ -4,15 +4,16 @@
 ``convolve``: ``texture``, ``u``, ``v``, ``kernel`` as float32 CUDA tensors,
 plus ``uv_mode``, ``boundaries``, ``iterations`` and optionally ``tile_x``),
 validates every item with the rules and messages of ``convolve``, and
-preallocates the outputs and one workspace.  ``run()`` makes one persistent
-kernel launch that runs the whole batch from a work queue (pack, traced
-pass and replays of every item, each level of an item waiting for its
-previous one; rlic_convolve_batch_f32), or, with ``per_level=True``, one
-pack launch and one launch per pass level over all items.  ``capture()``
+preallocates the outputs and one workspace.  ``run()`` makes one pack
+launch and one launch per pass level over all items
+(rlic_convolve_batch_f32), or, with ``queue=True``, one persistent kernel
+launch that runs the whole batch from a work queue (pack, traced pass and
+replays of every item, each level of an item waiting for its previous
+one).  ``capture()``
 records a run into a CUDA graph so that ``replay()`` re-runs the whole
 batch with a single graph launch; write new textures into the plan's input
 tensors in place between replays.  ``status()`` reports whether the last
-persistent run's bounded waits all ended.
+work-queue run's bounded waits all ended.
 
 ``autotune_tiles`` picks, per bucket of similar items (side, kernel length,
 uv mode), the CTA tile shape (``tile_x`` x 256 / ``tile_x`` pixels) and the
@@ -58,12 +59,12 @@ def _validate_item(k: int, item: dict) -> tuple:
 class BatchPlan:
     """Preallocated batch of convolutions (see the module docstring)."""
 
-    def __init__(self, items: list[dict], per_level: bool = False) -> None:
+    def __init__(self, items: list[dict], queue: bool = False) -> None:
         import torch
 
         if not items:
             raise ValueError("empty batch")
-        self.per_level = per_level
+        self.queue = queue
         self.lib = _native.lib()
         self.device = items[0]["texture"].device
         self.inputs: list[dict] = []
@@ -101,15 +102,15 @@ class BatchPlan:
 
         stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         flags = _native.RLIC_FLAG_BATCH_PREPARED if self.prepared else 0
-        if self.per_level:
-            flags |= _native.RLIC_FLAG_BATCH_PER_LEVEL
+        if self.queue:
+            flags |= _native.RLIC_FLAG_BATCH_QUEUE
         _native.check(self.lib.rlic_convolve_batch_f32(
             self.items, self.count, self.workspace.data_ptr(), self.nbytes, stream, flags))
         self.prepared = True
         return self.outputs
 
     def status(self) -> bool:
-        """True if every bounded wait of the last persistent run ended
+        """True if every bounded wait of the last work-queue run ended
         (synchronises the device)."""
         rc = self.lib.rlic_batch_status_f32(self.items, self.count, self.workspace.data_ptr())
         if rc < 0:
@@ -173,8 +174,8 @@ def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
 
     Each bucket is timed on its first item, as a one-item batch of at most
     two iterations (a traced pass and a replay): first the tile shapes, then,
-    with the best shape, the tiles per replay work item.  Returns the choice
-    per bucket.
+    with the best shape, the tiles per replay work item of the work-queue
+    form.  Returns the choice per bucket.
     """
     choice: dict = {}
     for item in items:
@@ -184,9 +185,10 @@ def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
             best_tx = min(candidates, key=lambda tx: _time_plan(
                 BatchPlan([{**probe, "tile_x": tx}]), repeats))
             best_rt = 0
-            if probe["iterations"] >= 2:
+            if probe["iterations"] >= 2:  # tiles per replay item of the work queue
                 best_rt = min(replay_candidates, key=lambda rt: _time_plan(
-                    BatchPlan([{**probe, "tile_x": best_tx, "replay_tiles": rt}]), repeats))
+                    BatchPlan([{**probe, "tile_x": best_tx, "replay_tiles": rt}], queue=True),
+                    repeats))
             choice[key] = (best_tx, best_rt)
         item["tile_x"], item["replay_tiles"] = choice[key]
     return choice

@@ -194,8 +194,11 @@ batch_gather_kernel(const BatchInstance* __restrict__ insts, BatchLevel lv, int 
 // Minimum resident CTAs per SM requested from the register allocator for
 // the persistent kernel (its registers are those of its costliest path, the
 // traced pass; the replays run at the same occupancy).
+// 6 (at most 40 registers): measured fastest of 4 (64 registers, the
+// compiler's choice), 5 and 6 on the 64-instance and 256-small-instance
+// mixes (small mix 19.4 / 11.7 / 11.7 ms, 64-instance mix 199 / 105 / 102 ms).
 #ifndef RLIC_BATCH_QUEUE_MIN_BLOCKS
-#define RLIC_BATCH_QUEUE_MIN_BLOCKS 1
+#define RLIC_BATCH_QUEUE_MIN_BLOCKS 6
 #endif
 
 constexpr int kQueueSegSmem = 2048;          // segment starts kept in shared memory

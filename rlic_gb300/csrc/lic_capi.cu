@@ -999,9 +999,9 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
     g_last_error.clear();
     int rc = batch_check(items, count);
     if (rc) return rc;
-    if (flags & ~unsigned(RLIC_FLAG_BATCH_PREPARED | RLIC_FLAG_BATCH_PER_LEVEL))
+    if (flags & ~unsigned(RLIC_FLAG_BATCH_PREPARED | RLIC_FLAG_BATCH_QUEUE))
         return fail(RLIC_ERR_INVALID_ARGUMENT,
-                    "this entry point takes RLIC_FLAG_BATCH_PREPARED and RLIC_FLAG_BATCH_PER_LEVEL only");
+                    "this entry point takes RLIC_FLAG_BATCH_PREPARED and RLIC_FLAG_BATCH_QUEUE only");
     if (!workspace) return fail(RLIC_ERR_INVALID_ARGUMENT, "the batched form needs a workspace");
     const BatchLayout L = batch_layout(items, count);
     if (workspace_bytes_ < L.total)
@@ -1124,7 +1124,7 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
                                           size_t(items[k].ny) * size_t(items[k].nx) * 4, stream));
     if (L.max_iterations == 0) return RLIC_OK;
     RLIC_CUDA_TRY(cudaMemsetAsync(ws + L.flags, 0, size_t(count) * sizeof(unsigned), stream));
-    if (flags & RLIC_FLAG_BATCH_PER_LEVEL) {
+    if (!(flags & RLIC_FLAG_BATCH_QUEUE)) {
         RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
         for (int level = 1; level <= L.max_iterations; ++level)
             RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));

@@ -1,7 +1,7 @@
 """Batched form: one call for many instances of uneven sizes, kernels,
 boundaries, uv modes and iteration counts, bit-identical to one convolve
 call per instance, also when replayed from a captured CUDA graph, both in
-one persistent launch from a work queue and with one launch per level."""
+with one launch per level and in one persistent launch from a work queue."""
 
 from __future__ import annotations
 
@@ -44,14 +44,14 @@ def _mixed_items():
     return items
 
 
-@pytest.mark.parametrize("per_level", [False, True], ids=["queue", "per-level"])
-def test_batch_matches_individual_calls(per_level) -> None:
+@pytest.mark.parametrize("queue", [False, True], ids=["per-level", "queue"])
+def test_batch_matches_individual_calls(queue) -> None:
     import torch
 
     items = _mixed_items()
     for k, it in enumerate(items):
         it["replay_tiles"] = [0, 1, 3, 64][k % 4]
-    plan = BatchPlan(items, per_level=per_level)
+    plan = BatchPlan(items, queue=queue)
     outs = plan.run()
     for it, got, want in zip(items, outs, _reference(items)):
         if it["iterations"] == 0:
@@ -71,21 +71,21 @@ def test_batch_queue_many_small_instances() -> None:
     items = batch_case(count=300, seed=13, min_side=16, max_side=96)
     for it in items:
         it["iterations"] = 10
-    plan = BatchPlan(items)
+    plan = BatchPlan(items, queue=True)
     outs = plan.run()
     for got, want in zip(outs, _reference(items)):
         assert torch.equal(got.view(torch.int32), want.view(torch.int32))
     assert plan.status()
 
 
-@pytest.mark.parametrize("per_level", [False, True], ids=["queue", "per-level"])
-def test_batch_graph_replay_with_new_textures(per_level) -> None:
+@pytest.mark.parametrize("queue", [False, True], ids=["per-level", "queue"])
+def test_batch_graph_replay_with_new_textures(queue) -> None:
     import torch
 
     items = _mixed_items()
     for it in items:
         it["iterations"] = max(it["iterations"], 1)
-    plan = BatchPlan(items, per_level=per_level)
+    plan = BatchPlan(items, queue=queue)
     plan.capture()
     for round_ in range(2):
         gen = torch.Generator(device="cuda").manual_seed(round_)
