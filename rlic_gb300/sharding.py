@@ -121,8 +121,13 @@ class HaloExchange:
         # this rank's own rows inside its extended band (several copies when
         # a periodic band wraps onto itself)
         own = [(q, int(g) - r0) for q, g in enumerate(ext) if plan.owner(int(g)) == rank]
-        self.own_dst = np.array([q for q, _ in own], dtype=np.int64)
-        self.own_src = np.array([k for _, k in own], dtype=np.int64)
+        off = plan.owned_offset[rank]
+        n_own = plan.bands[rank][1] - r0
+        # the copies outside the owned block (q != off + k)
+        copies = [(q, k) for q, k in own if q != off + k]
+        assert all(0 <= k < n_own for _, k in own)
+        self.copy_dst = np.array([q for q, _ in copies], dtype=np.int64)
+        self.copy_src = np.array([k for _, k in copies], dtype=np.int64)
         # per source rank: extended-band positions of its rows, in the order
         # of the rows it sends
         self.recv: dict[int, tuple[np.ndarray, np.ndarray]] = {}
@@ -151,13 +156,26 @@ class HaloExchange:
     def fill(self, owned, ext) -> None:
         """Writes the extended band `ext` (rows x nx torch tensor, in place)
         from `owned`, this rank's rows [r0, r1), and the other ranks' rows."""
+        off = self.plan.owned_offset[self.rank]
+        ext[off:off + owned.shape[0]].copy_(owned)
+        self.refresh(ext)
+
+    def refresh(self, ext) -> None:
+        """Rewrites the halo rows of the extended band `ext` in place, its
+        owned rows (at the plan's owned offset) being current: the copies of
+        owned rows a periodic band holds twice, and the other ranks' rows.
+        A pass's output band becomes the next pass's input this way, with no
+        copy of the owned rows."""
         import torch
         import torch.distributed as dist
 
-        dev = owned.device
+        off = self.plan.owned_offset[self.rank]
+        r0, r1 = self.plan.bands[self.rank]
+        owned = ext[off:off + (r1 - r0)]
+        dev = ext.device
         idx = lambda a: torch.from_numpy(a).to(dev)  # noqa: E731
-        if self.own_dst.size:
-            ext.index_copy_(0, idx(self.own_dst), owned.index_select(0, idx(self.own_src)))
+        if self.copy_dst.size:
+            ext.index_copy_(0, idx(self.copy_dst), owned.index_select(0, idx(self.copy_src)))
         if not self.transfers:  # a single rank: its band holds only its own rows
             return
         staged = self._staged(owned)
@@ -333,6 +351,6 @@ def convolve_row_sharded(texture, u, v, *, kernel, uv_mode="velocity", boundarie
     for it in range(iterations):
         out_ext = eng.first(tex_ext) if it == 0 else eng.next(tex_ext)
         if it + 1 < iterations:
-            tex_ext = torch.empty_like(out_ext)
-            halo.fill(out_ext[off:off + (r1 - r0)], tex_ext)
+            halo.refresh(out_ext)  # the output band, halo refreshed, is the next input
+            tex_ext = out_ext
     return r0, r1, out_ext[off:off + (r1 - r0)].cpu().numpy().copy()
