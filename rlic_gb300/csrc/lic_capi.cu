@@ -862,10 +862,19 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
         RLIC_CUDA_TRY(rlic::launch_lowp_prepare(kernel, int(klen), iterations, w32, inv_scale,
                                                 undo, stream));
         RLIC_CUDA_TRY(rlic::launch_to_storage(texture, bufs[0], storage, n, stream));
+        const int mode = g_replay_mode.load();
+        const bool staged =
+            mode == RLIC_REPLAY_STAGED || (mode == RLIC_REPLAY_AUTO && kStagedByDefault);
         for (int64_t it = 0; it < iterations; ++it) {
-            RLIC_CUDA_TRY(rlic::launch_gather_lowp(storage, bufs[it % 2], codes, w32, int(klen),
-                                                   inv_scale, sh, lc, bufs[(it + 1) % 2],
-                                                   stream));
+            cudaError_t e = cudaErrorNotSupported;
+            if (staged)
+                e = rlic::launch_gather_staged_lowp(storage, bufs[it % 2], codes, w32, int(klen),
+                                                    inv_scale, sh, nan_flag, bufs[(it + 1) % 2],
+                                                    stream);
+            if (e == cudaErrorNotSupported)
+                e = rlic::launch_gather_lowp(storage, bufs[it % 2], codes, w32, int(klen),
+                                             inv_scale, sh, lc, bufs[(it + 1) % 2], stream);
+            RLIC_CUDA_TRY(e);
         }
         RLIC_CUDA_TRY(rlic::launch_from_storage(bufs[iterations % 2], storage, undo, out, n,
                                                 stream));

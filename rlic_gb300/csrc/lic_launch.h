@@ -125,6 +125,13 @@ cudaError_t launch_gather_staged(bool fma, const double* tex_in, const uint32_t*
                                  const double* kernel, int klen, const Shape& sh,
                                  const unsigned* field_nan, double* tex_out,
                                  cudaStream_t stream);
+// The reduced-precision replay (FP16/BF16 cells, FP32 compensated sums)
+// with the same staging; cudaErrorNotSupported as above (rows must be a
+// multiple of 16 bytes of storage cells).
+cudaError_t launch_gather_staged_lowp(int storage, const void* tex_in, const uint32_t* codes,
+                                      const float* w32, int klen, const float* inv_scale,
+                                      const Shape& sh, const unsigned* field_nan,
+                                      void* tex_out, cudaStream_t stream);
 // Super-tile height of the staged replay, in pixels (a multiple of 4).
 void set_stage_rows(int rows);
 // Whether a staged replay ever gave up waiting for its copy.

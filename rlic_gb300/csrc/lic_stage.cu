@@ -27,8 +27,10 @@
 
 #include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
 #include "lic_kernels.cuh"
+#include "lic_lowp.cuh"
 
 namespace rlic {
 
@@ -297,6 +299,175 @@ lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __res
     }
 }
 
+// ----------------------------------- reduced-precision staged replay --
+//
+// The same staging for the FP16 / BF16 storage form (lic_lowp.cu): the box
+// holds 2-byte cells, each converted to FP32 when gathered, and the samples
+// accumulate by compensated (Kahan) summation in the order of the traced
+// pass, exactly as lic_gather_lowp_kernel does, so the results are the same
+// bits.
+
+__device__ __forceinline__ float stored_to_f32(__half h) { return __half2float(h); }
+__device__ __forceinline__ float stored_to_f32(__nv_bfloat16 h) { return __bfloat162float(h); }
+
+template <typename S>
+__device__ __forceinline__ void gather_word_lowp(int& cell, uint32_t wd, int pitch, const S* box,
+                                                 float x[8]) {
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        cell += box_delta(wd, b, pitch);
+        x[b] = stored_to_f32(box[cell]);
+    }
+}
+
+__device__ __forceinline__ void kahan_word(float& sum, float& comp, const float x[8],
+                                           const float* w) {
+    float wq[8];
+    load_weights8(w, wq);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) kahan_add(sum, comp, wq[b], x[b]);
+}
+
+// replay_half_staged with FP16/BF16 cells and compensated FP32 sums.
+template <typename S, bool STOPS>
+__device__ __forceinline__ void replay_half_staged_lowp(float& sum, float& comp, int cell,
+                                                        const uint32_t* __restrict__ words,
+                                                        int64_t npix, int count, uint32_t w0,
+                                                        uint32_t w1, const float* w, int pitch,
+                                                        const S* box) {
+    const int full = count >> 3;
+    const int nwords = (count + 7) >> 3;
+    int q = 0;
+    if (full > 0 && !(STOPS && word_has_stop(w0))) {
+        float x[8], y[8];
+        gather_word_lowp(cell, w0, pitch, box, x);
+        uint32_t wn = w1;
+        bool in_x = true;
+        for (q = 1; q < full;) {
+            uint32_t wd = wn;
+            wn = code_word(words, npix, q + 1, nwords);
+            if (STOPS && word_has_stop(wd)) break;
+            gather_word_lowp(cell, wd, pitch, box, y);
+            kahan_word(sum, comp, x, w + 8 * (q - 1));
+            in_x = false;
+            if (++q >= full) break;
+            wd = wn;
+            wn = code_word(words, npix, q + 1, nwords);
+            if (STOPS && word_has_stop(wd)) break;
+            gather_word_lowp(cell, wd, pitch, box, x);
+            kahan_word(sum, comp, y, w + 8 * (q - 1));
+            in_x = true;
+            ++q;
+        }
+        if (in_x) {
+            kahan_word(sum, comp, x, w + 8 * (q - 1));
+        } else {
+            kahan_word(sum, comp, y, w + 8 * (q - 1));
+        }
+    }
+    for (; q < nwords; ++q) {
+        const int n = (q < full) ? 8 : (count & 7);
+        const uint32_t wd = q == 0 ? w0 : (q == 1 ? w1 : code_word(words, npix, q, nwords));
+        const float* wq = w + 8 * q;
+        for (int b = 0; b < n; ++b) {
+            if (STOPS && ((wd >> (4 * b)) & 15u) == kStop) return;
+            cell += box_delta(wd, b, pitch);
+            kahan_add(sum, comp, wq[b], stored_to_f32(box[cell]));
+        }
+    }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kStageThreadsX * kStageThreadsY)
+lic_gather_staged_lowp_kernel(const __grid_constant__ CUtensorMap map,
+                              const S* __restrict__ tex_in, const uint32_t* __restrict__ codes,
+                              const float* __restrict__ w32, int klen,
+                              const float* __restrict__ inv_scale, Geometry<int32_t> g,
+                              StageGrid sg, S* __restrict__ tex_out, CodeLayout cl,
+                              const unsigned* __restrict__ field_nan) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+    S* box = reinterpret_cast<S*>(smem_raw + kStageBoxOffset);
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    const int nf_pad = (nf + 7) & ~7;
+    const int nb_pad = (kmid + 7) & ~7;
+    // weights after the box, 16-byte aligned
+    const size_t box_bytes_al = (size_t(sg.bw) * size_t(sg.bh) * sizeof(S) + 15) & ~size_t(15);
+    float* wsm = reinterpret_cast<float*>(smem_raw + kStageBoxOffset + box_bytes_al);
+    int* gtab = reinterpret_cast<int*>(wsm + nf_pad + nb_pad);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    load_step_weights(wsm, w32, klen, nf_pad);
+    if (tid == 0) {
+        fill_delta_table(gtab, g.nx, g.ny);
+        mbar_init(bar);
+    }
+    __syncthreads();
+    const float wmid = __ldg(w32 + kmid);
+    const float scale = __ldg(inv_scale);
+    const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
+    const uint32_t* codes_b = codes + size_t(cl.words_f) * size_t(cl.npix);
+    const uint32_t box_bytes = uint32_t(sg.bw) * uint32_t(sg.bh) * uint32_t(sizeof(S));
+    const int nwf = (nf + 7) >> 3, nwb = (kmid + 7) >> 3;
+    uint32_t parity = 0;
+    for (int tile = blockIdx.x; tile < sg.ntiles; tile += gridDim.x) {
+        const int ti = tile / sg.tiles_x;
+        const int tj = tile - ti * sg.tiles_x;
+        const int x0 = tj * sg.sx, y0 = ti * sg.sy;
+        const int bx0 = x0 - sg.hx, by0 = y0 - sg.hy;
+        const bool staged = !(sg.wrap_x && (bx0 < 0 || bx0 + sg.bw > g.nx)) &&
+                            !(sg.wrap_y && (by0 < 0 || by0 + sg.bh > g.ny));
+        if (staged) {
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(bar, box_bytes);
+                tma_load_box(box, &map, bx0, by0, bar);
+            }
+            const bool arrived = mbar_wait_bounded(bar, parity);
+            if (__syncthreads_or(!arrived)) {
+                if (tid == 0) atomicExch(&g_stage_timeout, 1u);
+                if (!arrived) mbar_wait_bounded(bar, parity);
+                return;
+            }
+            parity ^= 1u;
+        }
+        for (int r = threadIdx.y; r < sg.sy; r += kStageThreadsY) {
+            const int c = threadIdx.x;
+            const int i = y0 + r, j = x0 + c;
+            if (i >= g.ny || j >= g.nx) continue;
+            const int p = i * g.nx + j;
+            float sum = 0.f, comp = 0.f;
+            if (staged) {
+                const uint32_t f0 = code_word(codes + p, cl.npix, 0, nwf);
+                const uint32_t f1 = code_word(codes + p, cl.npix, 1, nwf);
+                const uint32_t b0 = code_word(codes_b + p, cl.npix, 0, nwb);
+                const uint32_t b1 = code_word(codes_b + p, cl.npix, 1, nwb);
+                const int cell = (r + sg.hy) * sg.bw + (c + sg.hx);
+                kahan_add(sum, comp, wmid, stored_to_f32(box[cell]));
+                if (nan_free) {
+                    replay_half_staged_lowp<S, false>(sum, comp, cell, codes + p, cl.npix, nf, f0,
+                                                      f1, wsm, sg.bw, box);
+                    replay_half_staged_lowp<S, false>(sum, comp, cell, codes_b + p, cl.npix, kmid,
+                                                      b0, b1, wsm + nf_pad, sg.bw, box);
+                } else {
+                    replay_half_staged_lowp<S, true>(sum, comp, cell, codes + p, cl.npix, nf, f0,
+                                                     f1, wsm, sg.bw, box);
+                    replay_half_staged_lowp<S, true>(sum, comp, cell, codes_b + p, cl.npix, kmid,
+                                                     b0, b1, wsm + nf_pad, sg.bw, box);
+                }
+            } else {
+                kahan_add(sum, comp, wmid, StorageTraits<S>::load(tex_in + p));
+                replay_half_lowp<S, int32_t>(sum, comp, p, codes + p, cl.npix, nf, wsm, gtab,
+                                             tex_in);
+                replay_half_lowp<S, int32_t>(sum, comp, p, codes_b + p, cl.npix, kmid,
+                                             wsm + nf_pad, gtab, tex_in);
+            }
+            tex_out[p] = StorageTraits<S>::from_float(__fmul_rn(sum, scale));
+        }
+        __syncthreads();
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn(cudaError_t* err) {
     static std::mutex mu;
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -331,53 +502,94 @@ int stage_pad() {
     return pad;
 }
 
+// Super-tile, halo and box of a staged replay of `elem`-byte cells, and the
+// tensor map over the texture; cudaErrorNotSupported when the image or the
+// kernel does not fit the form.
+cudaError_t plan_stage(const void* tex_in, size_t elem, CUtensorMapDataType dtype, int klen,
+                       const Shape& sh, size_t weights_bytes, StageGrid* sg, size_t* smem,
+                       CUtensorMap* map) {
+    const int kmid = klen / 2;
+    const int align = int(16 / elem);  // x of a copy: 16-byte aligned
+    if (!sh.small_index() || klen < 2 || (sh.nx * int64_t(elem)) % 16 != 0 ||
+        (reinterpret_cast<uintptr_t>(tex_in) & 15u) != 0)
+        return cudaErrorNotSupported;
+    sg->sx = kStageThreadsX;
+    sg->sy = g_stage_rows;
+    sg->hx = (kmid + align - 1) / align * align;
+    sg->hy = kmid;
+    sg->bw = sg->sx + 2 * sg->hx + (stage_pad() + align - 1) / align * align;
+    sg->bh = sg->sy + 2 * sg->hy;
+    if (sg->bw > 256 || sg->bh > 256) return cudaErrorNotSupported;  // box limit of a copy
+    sg->tiles_x = int(tiles_of(sh.nx, sg->sx));
+    const int64_t ntiles = int64_t(sg->tiles_x) * tiles_of(sh.ny, sg->sy);
+    if (ntiles > 0x7fffffffLL) return cudaErrorNotSupported;
+    sg->ntiles = int(ntiles);
+    sg->wrap_x = sh.bnd[0] == 1 || sh.bnd[1] == 1;
+    sg->wrap_y = sh.bnd[2] == 1 || sh.bnd[3] == 1;
+    const size_t box = (elem * size_t(sg->bw) * size_t(sg->bh) + 15) & ~size_t(15);
+    *smem = kStageBoxOffset + box + weights_bytes + 16 * sizeof(int);
+    if (*smem > 227 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = cudaSuccess;
+    auto encode = encode_fn(&e);
+    if (!encode) return e;
+    const cuuint64_t dims[2] = {cuuint64_t(sh.nx), cuuint64_t(sh.ny)};
+    const cuuint64_t strides[1] = {cuuint64_t(sh.nx) * elem};
+    const cuuint32_t boxdim[2] = {cuuint32_t(sg->bw), cuuint32_t(sg->bh)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult cr = encode(map, dtype, 2, const_cast<void*>(tex_in), dims, strides, boxdim,
+                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return cr == CUDA_SUCCESS ? cudaSuccess : cudaErrorNotSupported;
+}
+
+template <typename S>
+cudaError_t launch_gather_staged_lowp_t(const void* tex_in, const uint32_t* codes,
+                                        const float* w32, int klen, const float* inv_scale,
+                                        const Shape& sh, const unsigned* field_nan,
+                                        void* tex_out, cudaStream_t stream) {
+    const int kmid = klen / 2;
+    const int nf = klen - kmid - 1;
+    StageGrid sg;
+    size_t smem = 0;
+    CUtensorMap map;
+    const CUtensorMapDataType dt = sizeof(S) == 2 && std::is_same<S, __half>::value
+                                       ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                       : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    cudaError_t e = plan_stage(tex_in, sizeof(S), dt, klen, sh,
+                               sizeof(float) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7)), &sg,
+                               &smem, &map);
+    if (e != cudaSuccess) return e;
+    auto kfn = lic_gather_staged_lowp_kernel<S>;
+    unsigned grid = 0;
+    e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, sg.ntiles, &grid);
+    if (e != cudaSuccess) return e;
+    const auto g = make_geometry<int32_t>(sh);
+    const auto cl = make_code_layout(sh, klen);
+    kfn<<<grid, dim3(kStageThreadsX, kStageThreadsY), smem, stream>>>(
+        map, static_cast<const S*>(tex_in), codes, w32, klen, inv_scale, g, sg,
+        static_cast<S*>(tex_out), cl, field_nan);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <typename T, bool FMA>
 cudaError_t launch_gather_staged_t(const T* tex_in, const uint32_t* codes, const T* kernel,
                                    int klen, const Shape& sh, const unsigned* field_nan,
                                    T* tex_out, cudaStream_t stream) {
     const int kmid = klen / 2;
-    constexpr int align = int(16 / sizeof(T));  // x of a copy: 16-byte aligned
-    if (!sh.small_index() || klen < 2 || (sh.nx * int64_t(sizeof(T))) % 16 != 0 ||
-        (reinterpret_cast<uintptr_t>(tex_in) & 15u) != 0)
-        return cudaErrorNotSupported;
-    StageGrid sg;
-    sg.sx = kStageThreadsX;
-    sg.sy = g_stage_rows;
-    sg.hx = (kmid + align - 1) / align * align;
-    sg.hy = kmid;
-    sg.bw = sg.sx + 2 * sg.hx + stage_pad();
-    sg.bh = sg.sy + 2 * sg.hy;
-    if (sg.bw > 256 || sg.bh > 256) return cudaErrorNotSupported;  // box limit of a copy
-    sg.tiles_x = int(tiles_of(sh.nx, sg.sx));
-    const int64_t ntiles = int64_t(sg.tiles_x) * tiles_of(sh.ny, sg.sy);
-    if (ntiles > 0x7fffffffLL) return cudaErrorNotSupported;
-    sg.ntiles = int(ntiles);
-    sg.wrap_x = sh.bnd[0] == 1 || sh.bnd[1] == 1;
-    sg.wrap_y = sh.bnd[2] == 1 || sh.bnd[3] == 1;
     const int nf = klen - kmid - 1;
-    const size_t smem = kStageBoxOffset + sizeof(T) * size_t(sg.bw) * size_t(sg.bh) +
-                        sizeof(T) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7)) +
-                        16 * sizeof(int);
-    if (smem > 227 * 1024) return cudaErrorNotSupported;
-
-    cudaError_t e = cudaSuccess;
-    auto encode = encode_fn(&e);
-    if (!encode) return e;
+    StageGrid sg;
+    size_t smem = 0;
     CUtensorMap map;
-    const cuuint64_t dims[2] = {cuuint64_t(sh.nx), cuuint64_t(sh.ny)};
-    const cuuint64_t strides[1] = {cuuint64_t(sh.nx) * sizeof(T)};
-    const cuuint32_t box[2] = {cuuint32_t(sg.bw), cuuint32_t(sg.bh)};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult cr = encode(
-        &map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
-        2, const_cast<T*>(tex_in), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (cr != CUDA_SUCCESS) return cudaErrorNotSupported;
-
+    cudaError_t e = plan_stage(
+        tex_in, sizeof(T),
+        sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, klen,
+        sh, sizeof(T) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7)), &sg, &smem, &map);
+    if (e != cudaSuccess) return e;
     auto kfn = lic_gather_staged_kernel<T, FMA>;
     unsigned grid = 0;
-    e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, ntiles, &grid);
+    e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, sg.ntiles, &grid);
     if (e != cudaSuccess) return e;
     const auto g = make_geometry<int32_t>(sh);
     const auto cl = make_code_layout(sh, klen);
@@ -407,6 +619,19 @@ cudaError_t launch_gather_staged(bool fma, const double* tex_in, const uint32_t*
                                                       tex_out, stream)
                : launch_gather_staged_t<double, false>(tex_in, codes, kernel, klen, sh,
                                                        field_nan, tex_out, stream);
+}
+
+cudaError_t launch_gather_staged_lowp(int storage, const void* tex_in, const uint32_t* codes,
+                                      const float* w32, int klen, const float* inv_scale,
+                                      const Shape& sh, const unsigned* field_nan,
+                                      void* tex_out, cudaStream_t stream) {
+    if (storage == kStorageFP16)
+        return launch_gather_staged_lowp_t<__half>(tex_in, codes, w32, klen, inv_scale, sh,
+                                                   field_nan, tex_out, stream);
+    if (storage == kStorageBF16)
+        return launch_gather_staged_lowp_t<__nv_bfloat16>(tex_in, codes, w32, klen, inv_scale,
+                                                          sh, field_nan, tex_out, stream);
+    return cudaErrorInvalidValue;
 }
 
 void set_stage_rows(int rows) { g_stage_rows = rows; }

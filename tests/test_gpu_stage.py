@@ -181,3 +181,27 @@ def test_split_halves_through_host_arrays(oracle) -> None:
                               boundaries="periodic")
     want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], boundaries="periodic")
     assert _same_bits(got, want)
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("bnd", ["closed", {"x": "periodic", "y": "closed"}], ids=str)
+@pytest.mark.parametrize("shape", [(120, 200), (90, 134)])
+def test_staged_reduced_precision_replay(storage, dtype, bnd, shape) -> None:
+    """The FP16/BF16-storage form replays from TMA-staged boxes of 2-byte
+    cells (compensated FP32 sums in the traced pass's order): the same bits
+    as its L1 replay, NaN stops included.  134 columns are not a whole
+    number of 16-byte rows of 2-byte cells, so that call uses L1 throughout."""
+    from rlic_gb300.forms import convolve_lowp
+
+    tex, u, v = _field(*shape, dtype, seed=23, nans=True)
+    k = (1 - np.abs(np.linspace(-1, 1, 41))).astype(dtype)
+    kw = dict(kernel=k, uv_mode="polarization", boundaries=bnd, iterations=3, storage=storage)
+    try:
+        _native.set_replay_mode(_native.RLIC_REPLAY_STAGED)
+        got = convolve_lowp(tex, u, v, **kw)
+        _native.set_replay_mode(_native.RLIC_REPLAY_L1)
+        want = convolve_lowp(tex, u, v, **kw)
+    finally:
+        _native.set_replay_mode(_native.RLIC_REPLAY_AUTO)
+    assert _same_bits(got, want)
