@@ -645,6 +645,22 @@ __device__ __forceinline__ V ld_in(const V* p) {
     }
 }
 
+// 8 consecutive values from 16-byte aligned (shared) memory, with vector loads.
+__device__ __forceinline__ void load8_aligned(const float* w, float out[8]) {
+    const float4 a = reinterpret_cast<const float4*>(w)[0];
+    const float4 b = reinterpret_cast<const float4*>(w)[1];
+    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+}
+__device__ __forceinline__ void load8_aligned(const double* w, double out[8]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double2 a = reinterpret_cast<const double2*>(w)[k];
+        out[2 * k] = a.x;
+        out[2 * k + 1] = a.y;
+    }
+}
+
 // Per-trace state of convole_single_pixel (src/lib.rs:314-323).
 template <typename T, typename I>
 struct TraceState {
@@ -721,7 +737,10 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
     st.j = j;
     const int full = count >> 3;
     for (int q = 0; q < full; ++q) {
-        const T* wq = w + 8 * q;
+        // the word's 8 weights with 16-byte shared-memory loads (w is
+        // 16-byte aligned and every half starts on an 8-entry boundary)
+        T wq[8];
+        if constexpr (SAMPLE) load8_aligned(w + 8 * q, wq);
         uint32_t word = 0;
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
@@ -731,7 +750,8 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
                 if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                 return;
             }
-            word |= code << (4 * b);
+            // the 4-bit fields do not overlap: a multiply-add places the code
+            word += code * (1u << (4 * b));
         }
         if constexpr (RECORD) words[size_t(q) * stride] = word;
     }

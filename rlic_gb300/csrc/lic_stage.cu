@@ -108,23 +108,6 @@ __device__ __forceinline__ int box_delta(uint32_t wd, int b, int pitch) {
     return dy * pitch + dx;
 }
 
-// The 8 weights of one code word (8-entry aligned in shared memory) with
-// 16-byte loads; every lane reads the same address.
-__device__ __forceinline__ void load_weights8(const float* w, float out[8]) {
-    const float4 a = reinterpret_cast<const float4*>(w)[0];
-    const float4 b = reinterpret_cast<const float4*>(w)[1];
-    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
-    out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
-}
-__device__ __forceinline__ void load_weights8(const double* w, double out[8]) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const double2 a = reinterpret_cast<const double2*>(w)[k];
-        out[2 * k] = a.x;
-        out[2 * k + 1] = a.y;
-    }
-}
-
 // Word q of one half's codes (0 past the last word of the half).
 __device__ __forceinline__ uint32_t code_word(const uint32_t* __restrict__ words, int64_t npix,
                                               int q, int nwords) {
@@ -146,7 +129,7 @@ __device__ __forceinline__ void gather_word(int& cell, uint32_t wd, int pitch, c
 template <typename T, bool FMA>
 __device__ __forceinline__ void accumulate_word(T& acc, const T x[8], const T* w) {
     T wq[8];
-    load_weights8(w, wq);
+    load8_aligned(w, wq);
 #pragma unroll
     for (int b = 0; b < 8; ++b) acc = accumulate<T, FMA>(wq[b], x[b], acc);
 }
@@ -323,7 +306,7 @@ __device__ __forceinline__ void gather_word_lowp(int& cell, uint32_t wd, int pit
 __device__ __forceinline__ void kahan_word(float& sum, float& comp, const float x[8],
                                            const float* w) {
     float wq[8];
-    load_weights8(w, wq);
+    load8_aligned(w, wq);
 #pragma unroll
     for (int b = 0; b < 8; ++b) kahan_add(sum, comp, wq[b], x[b]);
 }
