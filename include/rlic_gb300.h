@@ -422,10 +422,11 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
 #define RLIC_REPLAY_STAGED 2
 RLIC_API int rlic_set_replay_mode(int mode, int stage_rows);
 /*
- * Images of at most max_pixels pixels (default 524288 = 2^19) trace their
- * first pass as split halves, one thread per half-streamline, recording the
- * path cache, and then replay it: on images too small to fill the GPU this
- * doubles the parallelism of the streamline arithmetic.  Bit-identical to
+ * Images of at most max_pixels pixels (default 0: none) trace their first
+ * pass as split halves, one thread per half-streamline, recording the path
+ * cache, and then replay it: on images too small to fill the GPU this
+ * doubles the parallelism of the streamline arithmetic, but on every size
+ * measured the extra replay cost more than that gained.  Bit-identical to
  * the single traced pass; 0 turns it off.  The workspace of such calls
  * holds the path cache even for one iteration (rlic_workspace_bytes counts
  * it under the setting in force), so change the setting only between calls

@@ -162,8 +162,12 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 #define RLIC_HOST_CHUNKS 8
 #endif
 
+// Off by default: on every size measured (128^2 to 1024^2, float32 and
+// float64, 1 and 5 passes) the split first pass and its replay were slower
+// than one fused traced pass (256^2 float64, one pass: 0.204 against
+// 0.160 ms; float32: 0.060 against 0.032 ms).
 #ifndef RLIC_SPLIT_PIXELS_DEFAULT
-#define RLIC_SPLIT_PIXELS_DEFAULT (1 << 19)
+#define RLIC_SPLIT_PIXELS_DEFAULT 0
 #endif
 
 // A non-blocking stream per device for the uploads of host-memory calls, at
@@ -280,8 +284,9 @@ Shape make_shape(int64_t ny, int64_t nx, const int bnd[4]) {
 
 // Images of at most this many pixels trace their first pass as split
 // halves (lic_record_halves_kernel, one thread per half-streamline) followed
-// by a replay: their tiles alone cannot fill the GPU, and the split doubles
-// the parallelism of the streamline arithmetic (rlic_set_split_pixels).
+// by a replay, which doubles the parallelism of the streamline arithmetic
+// where an image's tiles alone cannot fill the GPU (rlic_set_split_pixels;
+// off by default, see RLIC_SPLIT_PIXELS_DEFAULT).
 std::atomic<int64_t> g_split_pixels{RLIC_SPLIT_PIXELS_DEFAULT};
 
 int64_t split_pixels() { return g_split_pixels.load(); }

@@ -408,11 +408,10 @@ def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
     u, v = np.ascontiguousarray(c["u"]), np.ascontiguousarray(c["v"])
-    # texture check + pack + first pass (an image this small traces it as
-    # split halves, then replays it) + 2 replays, plus the texture upload as a
-    # gather kernel where the device reads host memory in place (else a
+    # texture check + pack + traced pass + 2 replays, plus the texture upload
+    # as a gather kernel where the device reads host memory in place (else a
     # copy-engine copy); one row chunk at this size
-    want = 7 if _native.lib().rlic_host_direct_access() else 6
+    want = 6 if _native.lib().rlic_host_direct_access() else 5
     rlic_gb300.convolve(c["texture"], u, v, kernel=c["kernel"], iterations=3)
     assert _native.launch_count() - before == want
     before = _native.launch_count()

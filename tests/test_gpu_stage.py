@@ -167,18 +167,22 @@ def test_split_halves_equal_the_traced_pass(oracle, dtype, bnd) -> None:
                                    iterations=iters)
             assert _same_bits(split, want), iters
     finally:
-        _native.set_split_pixels(1 << 19)
+        _native.set_split_pixels(0)
         _native.set_replay_mode(_native.RLIC_REPLAY_AUTO)
 
 
 def test_split_halves_through_host_arrays(oracle) -> None:
-    """The README case from numpy arrays (broadcast u, v read in place): the
-    host path splits the first pass of small images too."""
+    """The README case from numpy arrays (broadcast u, v read in place),
+    with the split first pass switched on: the host path splits too."""
     from rlic_gb300.workloads import readme_case
 
     c = readme_case()
-    got = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
-                              boundaries="periodic")
+    try:
+        _native.set_split_pixels(1 << 19)
+        got = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
+                                  boundaries="periodic")
+    finally:
+        _native.set_split_pixels(0)
     want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], boundaries="periodic")
     assert _same_bits(got, want)
 
