@@ -195,10 +195,10 @@ RLIC_API size_t rlic_batch_workspace_bytes_f32(const rlic_batch_item_f32 *items,
 RLIC_API int rlic_convolve_batch_f32(const rlic_batch_item_f32 *items, int count,
                                      void *workspace, size_t workspace_bytes, void *stream,
                                      unsigned flags);
-/* 1 if the last work-queue run of `items` on `workspace` gave up waiting for
- * a previous level (the bound guards against a fault; that run's results
- * are then incomplete), 0 if not, a negative error code on bad arguments.
- * Synchronises the device. */
+/* 1 if the last run of `items` on `workspace` was a work-queue run that gave
+ * up waiting for a previous level (the bound guards against a fault; that
+ * run's results are then incomplete), 0 if not, a negative error code on
+ * bad arguments.  Synchronises the device. */
 RLIC_API int rlic_batch_status_f32(const rlic_batch_item_f32 *items, int count,
                                    const void *workspace);
 

@@ -1138,13 +1138,15 @@ int convolve_batch_f32(const rlic_batch_item_f32* items, int count, void* worksp
                                           size_t(items[k].ny) * size_t(items[k].nx) * 4, stream));
     if (L.max_iterations == 0) return RLIC_OK;
     RLIC_CUDA_TRY(cudaMemsetAsync(ws + L.flags, 0, size_t(count) * sizeof(unsigned), stream));
+    // the queue's counters (and its timeout word, which rlic_batch_status_f32
+    // reads after either form) start at zero
+    RLIC_CUDA_TRY(cudaMemsetAsync(dev_counters, 0, size_t(L.nseg + 2) * sizeof(unsigned), stream));
     if (!(flags & RLIC_FLAG_BATCH_QUEUE)) {
         RLIC_CUDA_TRY(rlic::launch_batch_pack(dev_insts, count, max_pixels, stream));
         for (int level = 1; level <= L.max_iterations; ++level)
             RLIC_CUDA_TRY(rlic::launch_batch_level(dev_insts, levels[level], level, stream));
         return RLIC_OK;
     }
-    RLIC_CUDA_TRY(cudaMemsetAsync(dev_counters, 0, size_t(L.nseg + 2) * sizeof(unsigned), stream));
     rlic::BatchQueue q;
     q.seg_start = dev_seg_start;
     q.segs = dev_segs;

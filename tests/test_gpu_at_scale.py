@@ -280,7 +280,7 @@ def test_differentiable_workload_gradient_identities(dtype) -> None:
     L = float(loss.detach().double())
     adj = float((tex.grad.double() * t["texture"].double()).sum())
     euler = float((k.grad.double() * t["kernel"].double()).sum())
-    scale = float((out.abs() * W.abs()).sum().double())  # size of the sum's terms
+    scale = float((out.detach().abs() * W.abs()).sum().double())  # size of the sum's terms
     tol = 1e-10 if dtype == np.float64 else 2e-4
     assert abs(adj - L) <= tol * scale
     assert abs(euler - iters * L) <= tol * iters * scale
