@@ -445,7 +445,10 @@ RLIC_API int rlic_stage_timeouts(void);
 /*
  * Launch-shape tuning for the streamline kernels: CTA width and height in
  * pixels (block_x * block_y threads, at most 256; block_x a multiple of 32
- * or a divisor of 32).  Affects calls made after it on any thread.
+ * or a divisor of 32).  Affects calls made after it on any thread.  Until
+ * it is called, the library picks 64 x 4, and 16 x 4 for the traced passes
+ * of images of at most 2^19 pixels (more, smaller CTAs even the SMs' load
+ * when an image has few tiles).
  */
 RLIC_API int rlic_set_block_shape(int block_x, int block_y);
 

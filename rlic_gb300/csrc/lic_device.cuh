@@ -737,10 +737,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
     st.j = j;
     const int full = count >> 3;
     for (int q = 0; q < full; ++q) {
-        // the word's 8 weights with 16-byte shared-memory loads (w is
-        // 16-byte aligned and every half starts on an 8-entry boundary)
-        T wq[8];
-        if constexpr (SAMPLE) load8_aligned(w + 8 * q, wq);
+        const T* wq = w + 8 * q;
         uint32_t word = 0;
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
@@ -750,8 +747,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
                 if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                 return;
             }
-            // the 4-bit fields do not overlap: a multiply-add places the code
-            word += code * (1u << (4 * b));
+            word |= code << (4 * b);
         }
         if constexpr (RECORD) words[size_t(q) * stride] = word;
     }
