@@ -114,6 +114,24 @@ __device__ __forceinline__ uint32_t code_word(const uint32_t* __restrict__ words
     return q < nwords ? __ldg(words + size_t(q) * size_t(npix)) : 0u;
 }
 
+// Where a half's code words come from: global memory (word q of the pixel
+// at words[q * npix]) or a shared-memory copy of the super-tile's codes
+// (word q at words[q * stride]).
+struct GlobalWords {
+    const uint32_t* __restrict__ words;
+    int64_t npix;
+    __device__ __forceinline__ uint32_t operator()(int q, int nwords) const {
+        return code_word(words, npix, q, nwords);
+    }
+};
+struct SharedWords {
+    const uint32_t* words;
+    int stride;
+    __device__ __forceinline__ uint32_t operator()(int q, int nwords) const {
+        return q < nwords ? words[q * stride] : 0u;
+    }
+};
+
 // The 8 cells of one code word, gathered from the box into x.
 template <typename T>
 __device__ __forceinline__ void gather_word(int& cell, uint32_t wd, int pitch, const T* box,
@@ -144,12 +162,10 @@ __device__ __forceinline__ void accumulate_word(T& acc, const T x[8], const T* w
 // gathers are issued.  (Requesting four words ahead measured slower: the
 // extra registers cost a resident CTA.)  STOPS = false: the field holds no
 // NaN sample, so no word holds a stop code and none is tested.
-template <typename T, bool FMA, bool STOPS>
-__device__ __forceinline__ void replay_half_staged(T& acc, int cell,
-                                                   const uint32_t* __restrict__ words,
-                                                   int64_t npix, int count, uint32_t w0,
-                                                   uint32_t w1, const T* w, int pitch,
-                                                   const T* box) {
+template <typename T, bool FMA, bool STOPS, typename WS>
+__device__ __forceinline__ void replay_half_staged(T& acc, int cell, WS words, int count,
+                                                   uint32_t w0, uint32_t w1, const T* w,
+                                                   int pitch, const T* box) {
     const int full = count >> 3;
     const int nwords = (count + 7) >> 3;
     int q = 0;
@@ -160,14 +176,14 @@ __device__ __forceinline__ void replay_half_staged(T& acc, int cell,
         bool in_x = true;  // which buffer holds word q - 1, gathered, not yet accumulated
         for (q = 1; q < full;) {
             uint32_t wd = wn;
-            wn = code_word(words, npix, q + 1, nwords);
+            wn = words(q + 1, nwords);
             if (STOPS && word_has_stop(wd)) break;
             gather_word(cell, wd, pitch, box, y);
             accumulate_word<T, FMA>(acc, x, w + 8 * (q - 1));
             in_x = false;
             if (++q >= full) break;
             wd = wn;
-            wn = code_word(words, npix, q + 1, nwords);
+            wn = words(q + 1, nwords);
             if (STOPS && word_has_stop(wd)) break;
             gather_word(cell, wd, pitch, box, x);
             accumulate_word<T, FMA>(acc, y, w + 8 * (q - 1));
@@ -183,7 +199,7 @@ __device__ __forceinline__ void replay_half_staged(T& acc, int cell,
     // a word with a stop code, or the last partial word, step by step
     for (; q < nwords; ++q) {
         const int n = (q < full) ? 8 : (count & 7);
-        const uint32_t wd = q == 0 ? w0 : (q == 1 ? w1 : code_word(words, npix, q, nwords));
+        const uint32_t wd = q == 0 ? w0 : (q == 1 ? w1 : words(q, nwords));
         const T* wq = w + 8 * q;
         for (int b = 0; b < n; ++b) {
             if (STOPS && ((wd >> (4 * b)) & 15u) == kStop) return;
@@ -193,12 +209,49 @@ __device__ __forceinline__ void replay_half_staged(T& acc, int cell,
     }
 }
 
-template <typename T, bool FMA>
+// One staged pixel: the centre tap, then both halves, from word sources
+// `fw` (forward) and `bw` (backward).
+template <typename T, bool FMA, typename WS>
+__device__ __forceinline__ T staged_pixel(int cell, WS fw, WS bw, int nf, int kmid, T wmid,
+                                          const T* wsm, int nf_pad, int pitch, const T* box,
+                                          bool nan_free) {
+    const int nwf = (nf + 7) >> 3, nwb = (kmid + 7) >> 3;
+    // both halves' first two code words, four loads in flight
+    const uint32_t f0 = fw(0, nwf), f1 = fw(1, nwf);
+    const uint32_t b0 = bw(0, nwb), b1 = bw(1, nwb);
+    T acc = accumulate<T, FMA>(wmid, box[cell], T(0));
+    if (nan_free) {
+        replay_half_staged<T, FMA, false>(acc, cell, fw, nf, f0, f1, wsm, pitch, box);
+        replay_half_staged<T, FMA, false>(acc, cell, bw, kmid, b0, b1, wsm + nf_pad, pitch, box);
+    } else {
+        replay_half_staged<T, FMA, true>(acc, cell, fw, nf, f0, f1, wsm, pitch, box);
+        replay_half_staged<T, FMA, true>(acc, cell, bw, kmid, b0, b1, wsm + nf_pad, pitch, box);
+    }
+    return acc;
+}
+
+// A 3-D tiled copy of the super-tile's code words, box (64, sy, words) at
+// (x, y, 0), into shared memory.
+__device__ __forceinline__ void tma_load_codes(void* dst, const CUtensorMap* map, int x, int y,
+                                               uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(0), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// CODES: the super-tile's code words come into shared memory by a second
+// copy on the same mbarrier (a 3-D box over the word-major code array), so
+// no step waits on a code word from HBM.
+template <typename T, bool FMA, bool CODES>
 __global__ void __launch_bounds__(kStageThreadsX * kStageThreadsY)
-lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __restrict__ tex_in,
-                         const uint32_t* __restrict__ codes, const T* __restrict__ kernel,
-                         int klen, Geometry<int32_t> g, StageGrid sg, T* __restrict__ tex_out,
-                         CodeLayout cl, const unsigned* __restrict__ field_nan) {
+lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map,
+                         const __grid_constant__ CUtensorMap code_map,
+                         const T* __restrict__ tex_in, const uint32_t* __restrict__ codes,
+                         const T* __restrict__ kernel, int klen, Geometry<int32_t> g,
+                         StageGrid sg, T* __restrict__ tex_out, CodeLayout cl,
+                         const unsigned* __restrict__ field_nan) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
     T* box = reinterpret_cast<T*>(smem_raw + kStageBoxOffset);
@@ -206,7 +259,11 @@ lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __res
     const int nf = klen - kmid - 1;
     const int nf_pad = (nf + 7) & ~7;
     const int nb_pad = (kmid + 7) & ~7;
-    T* wsm = box + size_t(sg.bw) * size_t(sg.bh);
+    const int nwf = (nf + 7) >> 3, nwb = (kmid + 7) >> 3;
+    const size_t box_bytes_al = (size_t(sg.bw) * size_t(sg.bh) * sizeof(T) + 127) & ~size_t(127);
+    uint32_t* scodes = reinterpret_cast<uint32_t*>(smem_raw + kStageBoxOffset + box_bytes_al);
+    const uint32_t code_bytes = CODES ? uint32_t(kStageThreadsX * sg.sy * (nwf + nwb) * 4) : 0u;
+    T* wsm = reinterpret_cast<T*>(smem_raw + kStageBoxOffset + box_bytes_al + code_bytes);
     int* gtab = reinterpret_cast<int*>(wsm + nf_pad + nb_pad);  // image deltas
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     load_step_weights(wsm, kernel, klen, nf_pad);
@@ -220,7 +277,7 @@ lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __res
     const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
     const uint32_t* codes_b = codes + size_t(cl.words_f) * size_t(cl.npix);
     const uint32_t box_bytes = uint32_t(sg.bw) * uint32_t(sg.bh) * uint32_t(sizeof(T));
-    const int nwf = (nf + 7) >> 3, nwb = (kmid + 7) >> 3;
+    const int word_stride = kStageThreadsX * sg.sy;  // between a pixel's words in scodes
     uint32_t parity = 0;
     for (int tile = blockIdx.x; tile < sg.ntiles; tile += gridDim.x) {
         const int ti = tile / sg.tiles_x;
@@ -233,8 +290,9 @@ lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __res
             if (tid == 0) {
                 // order this CTA's earlier shared-memory reads before the copy
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(bar, box_bytes);
+                mbar_expect_tx(bar, box_bytes + code_bytes);
                 tma_load_box(box, &map, bx0, by0, bar);
+                if constexpr (CODES) tma_load_codes(scodes, &code_map, x0, y0, bar);
             }
             const bool arrived = mbar_wait_bounded(bar, parity);
             // the whole CTA leaves together if any thread gave up waiting
@@ -252,23 +310,16 @@ lic_gather_staged_kernel(const __grid_constant__ CUtensorMap map, const T* __res
             const int p = i * g.nx + j;
             T acc;
             if (staged) {
-                // both halves' first two code words, four loads in flight
-                const uint32_t f0 = code_word(codes + p, cl.npix, 0, nwf);
-                const uint32_t f1 = code_word(codes + p, cl.npix, 1, nwf);
-                const uint32_t b0 = code_word(codes_b + p, cl.npix, 0, nwb);
-                const uint32_t b1 = code_word(codes_b + p, cl.npix, 1, nwb);
                 const int cell = (r + sg.hy) * sg.bw + (c + sg.hx);
-                acc = accumulate<T, FMA>(wmid, box[cell], T(0));
-                if (nan_free) {
-                    replay_half_staged<T, FMA, false>(acc, cell, codes + p, cl.npix, nf, f0, f1,
-                                                      wsm, sg.bw, box);
-                    replay_half_staged<T, FMA, false>(acc, cell, codes_b + p, cl.npix, kmid, b0,
-                                                      b1, wsm + nf_pad, sg.bw, box);
+                if constexpr (CODES) {
+                    const uint32_t* mine = scodes + r * kStageThreadsX + c;
+                    acc = staged_pixel<T, FMA>(cell, SharedWords{mine, word_stride},
+                                               SharedWords{mine + nwf * word_stride, word_stride},
+                                               nf, kmid, wmid, wsm, nf_pad, sg.bw, box, nan_free);
                 } else {
-                    replay_half_staged<T, FMA, true>(acc, cell, codes + p, cl.npix, nf, f0, f1,
-                                                     wsm, sg.bw, box);
-                    replay_half_staged<T, FMA, true>(acc, cell, codes_b + p, cl.npix, kmid, b0,
-                                                     b1, wsm + nf_pad, sg.bw, box);
+                    acc = staged_pixel<T, FMA>(cell, GlobalWords{codes + p, cl.npix},
+                                               GlobalWords{codes_b + p, cl.npix}, nf, kmid, wmid,
+                                               wsm, nf_pad, sg.bw, box, nan_free);
                 }
             } else {
                 acc = accumulate<T, FMA>(wmid, __ldg(tex_in + p), T(0));
@@ -556,28 +607,71 @@ cudaError_t launch_gather_staged_lowp_t(const void* tex_in, const uint32_t* code
     return cudaGetLastError();
 }
 
+// Whether staged replays also copy their super-tile's code words into
+// shared memory (RLIC_STAGE_CODES=1 in the environment; tuning only).
+bool stage_codes() {
+    static const bool on = [] {
+        const char* e = std::getenv("RLIC_STAGE_CODES");
+        return e != nullptr && e[0] == '1';
+    }();
+    return on;
+}
+
 template <typename T, bool FMA>
 cudaError_t launch_gather_staged_t(const T* tex_in, const uint32_t* codes, const T* kernel,
                                    int klen, const Shape& sh, const unsigned* field_nan,
                                    T* tex_out, cudaStream_t stream) {
     const int kmid = klen / 2;
     const int nf = klen - kmid - 1;
+    const size_t wbytes = sizeof(T) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7));
     StageGrid sg;
     size_t smem = 0;
-    CUtensorMap map;
+    CUtensorMap map, code_map;
     cudaError_t e = plan_stage(
         tex_in, sizeof(T),
         sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, klen,
-        sh, sizeof(T) * size_t(((nf + 7) & ~7) + ((kmid + 7) & ~7)), &sg, &smem, &map);
+        sh, wbytes, &sg, &smem, &map);
     if (e != cudaSuccess) return e;
-    auto kfn = lic_gather_staged_kernel<T, FMA>;
+    const int words = int((nf + 7) / 8 + (kmid + 7) / 8);
+    bool with_codes = stage_codes() && sh.nx % 4 == 0 &&
+                      (reinterpret_cast<uintptr_t>(codes) & 15u) == 0 && words <= 256;
+    if (with_codes) {
+        const size_t box_al = (sizeof(T) * size_t(sg.bw) * size_t(sg.bh) + 127) & ~size_t(127);
+        const size_t smem_c = kStageBoxOffset + box_al +
+                              size_t(kStageThreadsX) * sg.sy * words * 4 + wbytes +
+                              16 * sizeof(int);
+        cudaError_t ce = cudaSuccess;
+        auto encode = encode_fn(&ce);
+        const cuuint64_t dims[3] = {cuuint64_t(sh.nx), cuuint64_t(sh.ny), cuuint64_t(words)};
+        const cuuint64_t strides[2] = {cuuint64_t(sh.nx) * 4,
+                                       cuuint64_t(sh.nx) * cuuint64_t(sh.ny) * 4};
+        const cuuint32_t boxdim[3] = {cuuint32_t(kStageThreadsX), cuuint32_t(sg.sy),
+                                      cuuint32_t(words)};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        with_codes = smem_c <= 227 * 1024 && encode != nullptr &&
+                     encode(&code_map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3,
+                            const_cast<uint32_t*>(codes), dims, strides, boxdim, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        if (with_codes) smem = smem_c;
+    }
+    if (!with_codes) code_map = map;  // unused
+    auto kfn = with_codes ? lic_gather_staged_kernel<T, FMA, true>
+                          : lic_gather_staged_kernel<T, FMA, false>;
+    if (!with_codes) {
+        // the layout without codes: the box rounded to 128 bytes, then weights
+        const size_t box_al = (sizeof(T) * size_t(sg.bw) * size_t(sg.bh) + 127) & ~size_t(127);
+        smem = kStageBoxOffset + box_al + wbytes + 16 * sizeof(int);
+        if (smem > 227 * 1024) return cudaErrorNotSupported;
+    }
     unsigned grid = 0;
     e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, sg.ntiles, &grid);
     if (e != cudaSuccess) return e;
     const auto g = make_geometry<int32_t>(sh);
     const auto cl = make_code_layout(sh, klen);
     kfn<<<grid, dim3(kStageThreadsX, kStageThreadsY), smem, stream>>>(
-        map, tex_in, codes, kernel, klen, g, sg, tex_out, cl, field_nan);
+        map, code_map, tex_in, codes, kernel, klen, g, sg, tex_out, cl, field_nan);
     count_launch();
     return cudaGetLastError();
 }
