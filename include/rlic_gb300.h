@@ -405,7 +405,8 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
  *   RLIC_REPLAY_L1      through L1 and L2 (lic_gather_kernel);
  *   RLIC_REPLAY_STAGED  from a box of cells around each 64 x stage_rows pixel
  *                       super-tile, copied into shared memory by the Tensor
- *                       Memory Accelerator; super-tiles whose box crosses a
+ *                       Memory Accelerator together with the super-tile's
+ *                       code words; super-tiles whose box crosses a
  *                       periodic edge, and images that do not fit the form
  *                       (rows not a multiple of 16 bytes, textures not in
  *                       device memory or not 16-byte aligned, boxes beyond
@@ -413,7 +414,7 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
  *                       2^31 pixels or more), use L1;
  *   RLIC_REPLAY_AUTO    the library's default (staged, where the image fits).
  * Both give bit-identical results.  stage_rows: super-tile height, a
- * multiple of 4 in [4, 64], or 0 for 24.  Affects calls made after it on any
+ * multiple of 4 in [4, 64], or 0 for 16.  Affects calls made after it on any
  * thread.  No counterpart in the reference (a tuning knob of this
  * implementation).
  */
@@ -446,9 +447,10 @@ RLIC_API int rlic_stage_timeouts(void);
  * Launch-shape tuning for the streamline kernels: CTA width and height in
  * pixels (block_x * block_y threads, at most 256; block_x a multiple of 32
  * or a divisor of 32).  Affects calls made after it on any thread.  Until
- * it is called, the library picks 64 x 4, and 16 x 4 for the traced passes
- * of images of at most 2^19 pixels (more, smaller CTAs even the SMs' load
- * when an image has few tiles).
+ * it is called, traced passes use 16 x 8 (8 x 8 for images of at most 2^19
+ * pixels: more CTAs even the SMs' load when an image has few tiles) and
+ * replays through L1 use 64 x 4; once called, every kernel uses the shape
+ * given.
  */
 RLIC_API int rlic_set_block_shape(int block_x, int block_y);
 

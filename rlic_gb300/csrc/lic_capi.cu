@@ -224,20 +224,22 @@ Variant make_variant(unsigned flags, int uv_mode) {
 
 LaunchConfig launch_config() { return LaunchConfig{g_block_x.load(), g_block_y.load()}; }
 
-// Whether rlic_set_block_shape chose the CTA shape; otherwise images of at
-// most kSmallImagePixels pixels trace with CTAs of 16 x 4 pixels: their
-// tiles are too few to spread evenly over the SMs in CTAs of 64 x 4, and
-// four times as many CTAs even the load (256^2 float64, one pass: 0.132
-// against 0.161 ms; 512^2 float32: 0.058 against 0.064 ms; at 8192^2 the
-// 64 x 4 CTAs are the faster).
+// CTA shape of the traced passes.  Unless rlic_set_block_shape chose one,
+// traced passes use squarer tiles than the replay's 64 x 4: 16 x 8 pixels,
+// and 8 x 8 for images of at most kSmallImagePixels pixels, whose tiles are
+// too few to spread evenly over the SMs otherwise.  Measured (ms per pass):
+// 8192^2 float32 with recording 9.78 against 10.18 for 64 x 4; 1024^2
+// float64 1.20 against 1.34; 256^2 float64 0.117 against 0.161; 512^2
+// float32 0.059 against 0.062.
 std::atomic<bool> g_block_custom{false};
 constexpr int64_t kSmallImagePixels = int64_t(1) << 19;
 
 LaunchConfig launch_config_for(int64_t ny, int64_t nx) {
     LaunchConfig lc = launch_config();
-    if (!g_block_custom.load() && ny * nx <= kSmallImagePixels) {
-        lc.block_x = 16;
-        lc.block_y = 4;
+    if (!g_block_custom.load()) {
+        const bool small = ny * nx <= kSmallImagePixels;
+        lc.block_x = small ? 8 : 16;
+        lc.block_y = 8;
     }
     return lc;
 }
@@ -266,7 +268,12 @@ cudaError_t replay_pass(bool fma, const T* src, const uint32_t* codes, const T* 
             if (e != cudaErrorNotSupported) return e;
         }
     }
-    return rlic::launch_gather(fma, src, codes, kernel, klen, sh, lc, dst, stream);
+    // the L1 replay keeps the library's CTA shape (64 x 4 unless set), not
+    // the traced passes' squarer tiles
+    LaunchConfig rl = lc;
+    rl.block_x = g_block_x.load();
+    rl.block_y = g_block_y.load();
+    return rlic::launch_gather(fma, src, codes, kernel, klen, sh, rl, dst, stream);
 }
 
 int check_shape(int64_t ny, int64_t nx, int64_t klen) {
@@ -896,7 +903,8 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
                                                     stream);
             if (e == cudaErrorNotSupported)
                 e = rlic::launch_gather_lowp(storage, bufs[it % 2], codes, w32, int(klen),
-                                             inv_scale, sh, lc, bufs[(it + 1) % 2], stream);
+                                             inv_scale, sh, launch_config(), bufs[(it + 1) % 2],
+                                             stream);
             RLIC_CUDA_TRY(e);
         }
         RLIC_CUDA_TRY(rlic::launch_from_storage(bufs[iterations % 2], storage, undo, out, n,
@@ -1528,7 +1536,7 @@ int rlic_set_replay_mode(int mode, int stage_rows) {
     if (stage_rows != 0 && (stage_rows < 4 || stage_rows > 64 || stage_rows % 4 != 0))
         return fail(RLIC_ERR_INVALID_ARGUMENT, "stage_rows must be 0 or a multiple of 4 in [4, 64]");
     g_replay_mode.store(mode);
-    rlic::set_stage_rows(stage_rows ? stage_rows : 24);
+    rlic::set_stage_rows(stage_rows ? stage_rows : 16);
     return RLIC_OK;
 }
 
