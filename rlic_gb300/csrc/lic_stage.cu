@@ -8,10 +8,12 @@
 // (SX + 2 HX) x (SY + 2 HY) cells around it, HX >= kmid and HY = kmid.  This
 // kernel is persistent: each CTA loops over super-tiles; for each one a
 // single thread issues one `cp.async.bulk.tensor.2d` copy of the box from HBM
-// (through L2) into shared memory, completing on an mbarrier, and the CTA
-// then replays its pixels from shared memory.  The copy engine fills the box,
-// so the fill costs the load/store pipe nothing; the gathers, which bound the
-// L1-cached replay, become shared-memory loads.
+// (through L2) into shared memory, and one `cp.async.bulk.tensor.3d` copy of
+// the super-tile's code words (all words of its pixels), both completing on
+// one mbarrier, and the CTA then replays its pixels from shared memory.  The
+// copy engine fills the box and the codes, so the fill costs the load/store
+// pipe nothing; the gathers, which bound the L1-cached replay, become
+// shared-memory loads, and no step waits on a code word from HBM.
 //
 // Super-tiles whose box would cross a periodic image edge (their streamlines
 // may wrap to the far side) replay through L1/L2 as lic_gather_kernel does.
