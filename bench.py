@@ -806,9 +806,11 @@ def run_batched(args) -> None:
     """Two batched mixes (rlic_gb300.workloads.batch_case): the 64-instance
     workload (sides 256-4096, seed 3) and 256 small instances (sides
     128-512, seed 5), each with kernels of 17-129 taps and 1-10 iterations.
-    Per mix: one launch per level (tuned tiles, also replayed from a CUDA
-    graph), the persistent work-queue launch, and one rlic_convolve_f32 call
-    per instance in its path-cache and plain forms."""
+    Per mix: the batched call (items of 2^21 pixels and more as their own
+    calls, the rest in one launch per level with tuned tiles; also replayed
+    from a CUDA graph), every item batched per level, every item in the
+    persistent work-queue launch, and one rlic_convolve_f32 call per
+    instance in its path-cache and plain forms."""
     import torch
 
     from rlic_gb300 import _native
@@ -834,7 +836,9 @@ def run_batched(args) -> None:
         ms_levels = _time_calls(plan.run, steps, args.warmup, stream)
         plan.capture()
         ms_graph = _time_calls(plan.replay, steps, args.warmup, stream)
-        queue = BatchPlan(items, queue=True)
+        every = BatchPlan(items, solo_pixels=0)
+        ms_every = _time_calls(every.run, steps, args.warmup, stream)
+        queue = BatchPlan(items, queue=True, solo_pixels=0)
         ms_queue = _time_calls(queue.run, steps, args.warmup, stream)
         assert queue.status(), "a bounded wait of the work queue gave up"
         seq = []
@@ -858,16 +862,19 @@ def run_batched(args) -> None:
 
         ms_seq = _time_calls(sequential(0), steps, args.warmup, stream)
         ms_seq_plain = _time_calls(sequential(_native.RLIC_FLAG_NO_PATH_CACHE), 2, 1, stream)
-        for (_, _, _, _, _, _, _, out), a, b in zip(seq, plan.outputs, queue.outputs):
-            assert torch.equal(out, a) and torch.equal(out, b), "batched result differs"
+        for (_, _, _, _, _, _, _, out), a, b, c in zip(seq, plan.outputs, queue.outputs,
+                                                      every.outputs):
+            assert torch.equal(out, a) and torch.equal(out, b) and torch.equal(out, c), \
+                "batched result differs"
         return {
             "instances": len(items),
             "pixels": int(sum(int(i["texture"].numel()) for i in items)),
             "samples_per_step": samples,
             "forms": {
-                "per_level_graph_replay": {"ms": ms_graph, "value": gs(samples, ms_graph)},
-                "per_level_call": {"ms": ms_levels, "value": gs(samples, ms_levels)},
-                "queue_call": {"ms": ms_queue, "value": gs(samples, ms_queue)},
+                "batched_graph_replay": {"ms": ms_graph, "value": gs(samples, ms_graph)},
+                "batched_call": {"ms": ms_levels, "value": gs(samples, ms_levels)},
+                "every_item_batched_per_level": {"ms": ms_every, "value": gs(samples, ms_every)},
+                "every_item_batched_queue": {"ms": ms_queue, "value": gs(samples, ms_queue)},
                 "sequential_path_cache_calls": {"ms": ms_seq, "value": gs(samples, ms_seq)},
                 "sequential_plain_calls": {"ms": ms_seq_plain,
                                            "value": gs(samples, ms_seq_plain)},
@@ -881,7 +888,7 @@ def run_batched(args) -> None:
         "batch_256_small_instances_seed5": measure(
             batch_case(count=256, seed=5, min_side=128, max_side=512)),
     }
-    head = mixes["batch_64_instances_seed3"]["forms"]["per_level_graph_replay"]["value"]
+    head = mixes["batch_64_instances_seed3"]["forms"]["batched_graph_replay"]["value"]
     print(json.dumps({
         "metric": METRIC, "unit": UNIT, "workload": "batch_64_instances_seed3",
         "value": head, "dtype": "f32", "mixes": mixes,

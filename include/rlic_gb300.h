@@ -410,8 +410,9 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
  *                       periodic edge, and images that do not fit the form
  *                       (rows not a multiple of 16 bytes, textures not in
  *                       device memory or not 16-byte aligned, boxes beyond
- *                       256 cells a side or the shared memory of a CTA,
- *                       2^31 pixels or more), use L1;
+ *                       256 cells a side or beyond 113 KB of shared memory,
+ *                       which would leave one CTA per SM, 2^31 pixels or
+ *                       more), use L1;
  *   RLIC_REPLAY_AUTO    the library's default (staged, where the image fits).
  * Both give bit-identical results.  stage_rows: super-tile height, a
  * multiple of 4 in [4, 64], or 0 for 16.  Affects calls made after it on any

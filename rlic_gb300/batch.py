@@ -15,6 +15,11 @@ batch with a single graph launch; write new textures into the plan's input
 tensors in place between replays.  ``status()`` reports whether the last
 work-queue run's bounded waits all ended.
 
+Items of at least ``SOLO_PIXELS`` pixels run as their own
+rlic_convolve_f32 calls in the same stream (and graph): such an item fills
+the GPU alone, and a single call replays from TMA-staged boxes, which the
+batched kernels do not (``solo_pixels=0`` batches every item).
+
 ``autotune_tiles`` picks, per bucket of similar items (side, kernel length,
 uv mode), the CTA tile shape (``tile_x`` x 256 / ``tile_x`` pixels) and the
 tiles per replay work item (``replay_tiles``) by timing the candidates on
@@ -34,6 +39,8 @@ from rlic_gb300 import _native
 from rlic_gb300._lib import _collect_problems, _Ops
 
 TILE_CANDIDATES = (64, 32, 16)
+# items of at least this many pixels (1448^2) run as their own calls
+SOLO_PIXELS = 1 << 21
 REPLAY_TILE_CANDIDATES = (2, 4, 8)
 
 
@@ -57,9 +64,18 @@ def _validate_item(k: int, item: dict) -> tuple:
 
 
 class BatchPlan:
-    """Preallocated batch of convolutions (see the module docstring)."""
+    """Preallocated batch of convolutions (see the module docstring).
 
-    def __init__(self, items: list[dict], queue: bool = False) -> None:
+    Items of at least ``solo_pixels`` pixels fill the GPU on their own, and
+    one call each (whose replays read TMA-staged boxes) runs them faster
+    than the batched kernels: those items run as their own
+    rlic_convolve_f32 calls, in the same stream (and the same captured
+    graph) as the batched call of the others.  ``solo_pixels=0`` batches
+    every item.
+    """
+
+    def __init__(self, items: list[dict], queue: bool = False,
+                 solo_pixels: int = SOLO_PIXELS) -> None:
         import torch
 
         if not items:
@@ -69,7 +85,7 @@ class BatchPlan:
         self.device = items[0]["texture"].device
         self.inputs: list[dict] = []
         self.outputs: list[Any] = []
-        arr = (_native.BatchItemF32 * len(items))()
+        batched, self.solo, total = [], [], 0
         for k, item in enumerate(items):
             bs = _validate_item(k, item)
             t = {x: item[x].to(device=self.device).contiguous() for x in ("texture", "u", "v", "kernel")}
@@ -77,41 +93,59 @@ class BatchPlan:
             self.inputs.append(t)
             self.outputs.append(out)
             ny, nx = t["texture"].shape
+            klen, iters = int(t["kernel"].shape[0]), int(item.get("iterations", 1))
+            total += ny * nx * klen * iters
+            mode = _native.UV_MODE_CODES[item.get("uv_mode", "velocity")]
+            if solo_pixels and ny * nx >= solo_pixels and iters >= 1:
+                self.solo.append((t, out, ny, nx, klen, iters, mode, bs.codes()))
+                continue
             xl, xr, yl, yr = bs.codes()
-            arr[k] = _native.BatchItemF32(
+            batched.append(_native.BatchItemF32(
                 t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(),
-                t["kernel"].data_ptr(), out.data_ptr(), ny, nx, t["kernel"].shape[0],
-                int(item.get("iterations", 1)),
-                _native.UV_MODE_CODES[item.get("uv_mode", "velocity")], xl, xr, yl, yr,
-                int(item.get("tile_x", 0)), int(item.get("replay_tiles", 0)),
-            )
-        self.items = arr
-        self.count = len(items)
-        nbytes = self.lib.rlic_batch_workspace_bytes_f32(self.items, self.count)
+                t["kernel"].data_ptr(), out.data_ptr(), ny, nx, klen, iters, mode, xl, xr, yl,
+                yr, int(item.get("tile_x", 0)), int(item.get("replay_tiles", 0)),
+            ))
+        self.total_samples = total
+        self.count = len(batched)
+        self.items = (_native.BatchItemF32 * max(self.count, 1))(*batched)
+        nbytes = self.lib.rlic_batch_workspace_bytes_f32(self.items, self.count) \
+            if self.count else 0
         self.workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
         self.nbytes = nbytes
+        self.solo_bytes = max((self.lib.rlic_workspace_bytes(ny, nx, klen, iters, 4, 0)
+                               for _, _, ny, nx, klen, iters, _, _ in self.solo), default=0)
+        self.solo_ws = torch.empty(max(self.solo_bytes, 1), dtype=torch.uint8,
+                                   device=self.device)
         self.prepared = False
         self.graph = None
 
     def samples(self) -> int:
-        return sum(int(it.ny * it.nx * it.klen * it.iterations) for it in self.items)
+        return self.total_samples
 
     def run(self) -> list:
         """Launch the batch on the current stream; returns the output tensors."""
         import torch
 
         stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
-        flags = _native.RLIC_FLAG_BATCH_PREPARED if self.prepared else 0
-        if self.queue:
-            flags |= _native.RLIC_FLAG_BATCH_QUEUE
-        _native.check(self.lib.rlic_convolve_batch_f32(
-            self.items, self.count, self.workspace.data_ptr(), self.nbytes, stream, flags))
+        for t, out, ny, nx, klen, iters, mode, bc in self.solo:
+            _native.check(self.lib.rlic_convolve_f32(
+                t["texture"].data_ptr(), t["u"].data_ptr(), t["v"].data_ptr(), ny, nx,
+                t["kernel"].data_ptr(), klen, mode, *bc, iters, out.data_ptr(),
+                self.solo_ws.data_ptr(), self.solo_bytes, stream, 0))
+        if self.count:
+            flags = _native.RLIC_FLAG_BATCH_PREPARED if self.prepared else 0
+            if self.queue:
+                flags |= _native.RLIC_FLAG_BATCH_QUEUE
+            _native.check(self.lib.rlic_convolve_batch_f32(
+                self.items, self.count, self.workspace.data_ptr(), self.nbytes, stream, flags))
         self.prepared = True
         return self.outputs
 
     def status(self) -> bool:
         """True if every bounded wait of the last work-queue run ended
         (synchronises the device)."""
+        if not self.count:
+            return True
         rc = self.lib.rlic_batch_status_f32(self.items, self.count, self.workspace.data_ptr())
         if rc < 0:
             _native.check(-rc)
@@ -183,12 +217,12 @@ def autotune_tiles(items: list[dict], candidates: tuple = TILE_CANDIDATES,
         if key not in choice:
             probe = {**item, "iterations": min(int(item.get("iterations", 1)), 2)}
             best_tx = min(candidates, key=lambda tx: _time_plan(
-                BatchPlan([{**probe, "tile_x": tx}]), repeats))
+                BatchPlan([{**probe, "tile_x": tx}], solo_pixels=0), repeats))
             best_rt = 0
             if probe["iterations"] >= 2:  # tiles per replay item of the work queue
                 best_rt = min(replay_candidates, key=lambda rt: _time_plan(
-                    BatchPlan([{**probe, "tile_x": best_tx, "replay_tiles": rt}], queue=True),
-                    repeats))
+                    BatchPlan([{**probe, "tile_x": best_tx, "replay_tiles": rt}], queue=True,
+                              solo_pixels=0), repeats))
             choice[key] = (best_tx, best_rt)
         item["tile_x"], item["replay_tiles"] = choice[key]
     return choice

@@ -42,6 +42,11 @@ constexpr int kStageThreadsX = 64;  // CTA: 64 x 4 threads, one column per threa
 constexpr int kStageThreadsY = 4;
 constexpr int kStageBoxOffset = 128;  // box start in shared memory (after the mbarrier)
 constexpr uint32_t kStageWaitLimit = 1u << 22;
+// The staged form needs at least two resident CTAs per SM to hide a copy
+// behind the other CTA's work: a box larger than this (129 float64 taps)
+// replays through L1 instead, which measured faster than one CTA per SM
+// (the 8192^2 float64, 129-tap path cache: 270 against 301 ms).
+constexpr size_t kStageMaxSmem = 113 * 1024;
 
 __device__ unsigned g_stage_timeout = 0u;
 
@@ -564,7 +569,7 @@ cudaError_t plan_stage(const void* tex_in, size_t elem, CUtensorMapDataType dtyp
     sg->wrap_y = sh.bnd[2] == 1 || sh.bnd[3] == 1;
     const size_t box = (elem * size_t(sg->bw) * size_t(sg->bh) + 15) & ~size_t(15);
     *smem = kStageBoxOffset + box + weights_bytes + 16 * sizeof(int);
-    if (*smem > 227 * 1024) return cudaErrorNotSupported;
+    if (*smem > kStageMaxSmem) return cudaErrorNotSupported;
     cudaError_t e = cudaSuccess;
     auto encode = encode_fn(&e);
     if (!encode) return e;
@@ -652,7 +657,7 @@ cudaError_t launch_gather_staged_t(const T* tex_in, const uint32_t* codes, const
         const cuuint32_t boxdim[3] = {cuuint32_t(kStageThreadsX), cuuint32_t(sg.sy),
                                       cuuint32_t(words)};
         const cuuint32_t estr[3] = {1, 1, 1};
-        with_codes = smem_c <= 227 * 1024 && encode != nullptr &&
+        with_codes = smem_c <= kStageMaxSmem && encode != nullptr &&
                      encode(&code_map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3,
                             const_cast<uint32_t*>(codes), dims, strides, boxdim, estr,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -667,7 +672,7 @@ cudaError_t launch_gather_staged_t(const T* tex_in, const uint32_t* codes, const
         // the layout without codes: the box rounded to 128 bytes, then weights
         const size_t box_al = (sizeof(T) * size_t(sg.bw) * size_t(sg.bh) + 127) & ~size_t(127);
         smem = kStageBoxOffset + box_al + wbytes + 16 * sizeof(int);
-        if (smem > 227 * 1024) return cudaErrorNotSupported;
+        if (smem > kStageMaxSmem) return cudaErrorNotSupported;
     }
     unsigned grid = 0;
     e = persistent_grid(kfn, kStageThreadsX * kStageThreadsY, smem, sg.ntiles, &grid);

@@ -112,3 +112,22 @@ def test_batch_validates_items() -> None:
     items[1]["uv_mode"] = "astral"
     with pytest.raises(ValueError, match=r"^Invalid uv_mode 'astral'"):
         BatchPlan(items)
+
+
+def test_large_items_run_as_their_own_calls() -> None:
+    """Items above the solo size run as single calls beside the batched call
+    of the others: the same bits as batching every item, also from a graph."""
+    import torch
+
+    items = batch_case(count=6, seed=17, min_side=96, max_side=400)
+    solo = BatchPlan(items, solo_pixels=150 * 150)
+    assert 0 < len(solo.solo) < len(items)
+    every = BatchPlan(items, solo_pixels=0)
+    a, b = solo.run(), every.run()
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+    solo.capture()
+    for x, y in zip(solo.replay(), b):
+        torch.cuda.synchronize()
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))

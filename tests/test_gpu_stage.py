@@ -79,8 +79,9 @@ def test_staged_equals_l1_and_oracle(oracle, staged, dtype, bnd, shape) -> None:
 @pytest.mark.parametrize("klen", [2, 9, 64, 65, 129, 191])
 @pytest.mark.parametrize("rows", [4, 32, 64])
 def test_staged_kernel_lengths_and_tile_heights(staged, klen, rows) -> None:
-    # 129 and 191 taps: boxes of 192 and 256 cells a side (float32), or
-    # beyond the shared memory of a CTA (the call then uses L1)
+    # 129 and 191 taps: boxes of 192 and 256 cells a side, most of them
+    # beyond the shared memory that leaves two CTAs per SM (the call then
+    # replays through L1)
     for dtype in (np.float32, np.float64):
         tex, u, v = _field(300, 264, dtype, seed=klen, nans=True)
         k = (1 - np.abs(np.linspace(-1, 1, klen + 2)[1:-1])).astype(dtype)
