@@ -436,6 +436,86 @@ sliding_smem_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins, i
     out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
 }
 
+// The same counts with each thread ranking kSlideRows vertically adjacent
+// pixels: their windows share all but kSlideRows - 1 rows, so every bin
+// loaded from shared memory is compared with up to kSlideRows pixel bins
+// (one load serves several compares, where sliding_smem_kernel loads each
+// bin once per pixel).  A CTA covers 32 x (8 * kSlideRows) pixels.
+constexpr int kSlideRows = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(kSlideBx * kSlideBy)
+sliding_smem_rows_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins, int64_t ny,
+                         int64_t nx, int th, int tw, const Stats<T>* st, T* __restrict__ out) {
+    extern __shared__ int32_t s_bins[];
+    constexpr int kTileY = kSlideBy * kSlideRows;
+    const int rw = kSlideBx + tw - 1, rh = kTileY + th - 1;  // region
+    const int64_t j0 = int64_t(blockIdx.x) * kSlideBx, i0 = int64_t(blockIdx.y) * kTileY;
+    const int64_t ri0 = i0 - th / 2, rj0 = j0 - tw / 2;
+    const int tid = threadIdx.y * kSlideBx + threadIdx.x;
+    for (int q = tid; q < rw * rh; q += kSlideBx * kSlideBy) {
+        const int qr = q / rw, qc = q - qr * rw;
+        const int64_t gi = ri0 + qr, gj = rj0 + qc;
+        s_bins[q] = (gi >= 0 && gi < ny && gj >= 0 && gj < nx) ? __ldg(bins + gi * nx + gj) : -1;
+    }
+    __syncthreads();
+    const int64_t j = j0 + threadIdx.x;
+    if (j >= nx) return;
+    // this thread's pixels: rows ty0 .. ty0 + kSlideRows - 1 of the tile
+    const int ty0 = threadIdx.y * kSlideRows;
+    uint32_t ub[kSlideRows], below[kSlideRows];
+#pragma unroll
+    for (int k = 0; k < kSlideRows; ++k) {
+        // -1 (a non-finite pixel, or a row below the image) ranks nothing
+        // useful; its count is discarded below
+        ub[k] = uint32_t(s_bins[(ty0 + k + th / 2) * rw + threadIdx.x + tw / 2]);
+        below[k] = 0;
+    }
+    const bool all_finite = st->count == (unsigned long long)(ny * nx);
+    // region row ty0 + r lies in the window of pixel k when k <= r < k + th
+    uint32_t valid_acc[kSlideRows];
+#pragma unroll
+    for (int k = 0; k < kSlideRows; ++k) valid_acc[k] = 0;
+    for (int r = 0; r < th + kSlideRows - 1; ++r) {
+        const int32_t* row = s_bins + (ty0 + r) * rw + threadIdx.x;
+        uint32_t cnt[kSlideRows];
+#pragma unroll
+        for (int k = 0; k < kSlideRows; ++k) cnt[k] = 0;
+        uint32_t nvalid = 0;
+        for (int c = 0; c < tw; ++c) {
+            const uint32_t v = uint32_t(row[c]);
+#pragma unroll
+            for (int k = 0; k < kSlideRows; ++k) cnt[k] += v <= ub[k];
+            if (!all_finite) nvalid += int32_t(v) >= 0;
+        }
+#pragma unroll
+        for (int k = 0; k < kSlideRows; ++k) {
+            const bool in = r >= k && r < k + th;
+            below[k] += in ? cnt[k] : 0u;
+            valid_acc[k] += in ? nvalid : 0u;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kSlideRows; ++k) {
+        const int64_t i = i0 + ty0 + k;
+        if (i >= ny) break;
+        const int64_t idx = i * nx + j;
+        if (int32_t(ub[k]) < 0) {
+            out[idx] = x[idx];
+            continue;
+        }
+        uint32_t valid = valid_acc[k];
+        if (all_finite) {  // the window clipped to the image
+            const int64_t r0 = i - th / 2 < 0 ? 0 : i - th / 2;
+            const int64_t r1 = i - th / 2 + th > ny ? ny : i - th / 2 + th;
+            const int64_t c0 = j - tw / 2 < 0 ? 0 : j - tw / 2;
+            const int64_t c1 = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
+            valid = uint32_t((r1 - r0) * (c1 - c0));
+        }
+        out[idx] = div_rn_(from_count<T>(below[k]), from_count<T>(valid));
+    }
+}
+
 unsigned grid_for(int64_t n) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 8) blocks = 152 * 8;
@@ -512,8 +592,21 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
         count_launch();
     } else {
         const int64_t gy = (ny + 7) / 8;
+        const int64_t gy_rows = (ny + kSlideBy * kSlideRows - 1) / (kSlideBy * kSlideRows);
         const size_t smem = size_t(kSlideBx + tw - 1) * size_t(kSlideBy + th - 1) * 4;
-        if (smem <= 200 * 1024 && gy <= 65535) {
+        const size_t smem_rows =
+            size_t(kSlideBx + tw - 1) * size_t(kSlideBy * kSlideRows + th - 1) * 4;
+        if (smem_rows <= 200 * 1024 && gy_rows <= 65535) {
+            auto kfn = sliding_smem_rows_kernel<T>;
+            if (smem_rows > 48 * 1024) {
+                e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem_rows));
+                if (e != cudaSuccess) return e;
+            }
+            kfn<<<dim3(unsigned((nx + kSlideBx - 1) / kSlideBx), unsigned(gy_rows)),
+                  dim3(kSlideBx, kSlideBy), smem_rows, stream>>>(x, bins, ny, nx, int(th),
+                                                                 int(tw), st, out);
+        } else if (smem <= 200 * 1024 && gy <= 65535) {
             auto kfn = sliding_smem_kernel<T>;
             if (smem > 48 * 1024) {
                 e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -105,3 +105,16 @@ def test_full_size_global_properties() -> None:
     cdf = torch.cumsum(counts, 0).to(torch.float64)
     torch.testing.assert_close(vals.double(), cdf / (n * n), rtol=1e-6, atol=0)
     assert len(vals) <= nbins
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("window", [(65, 65), (33, 17), (4, 9)], ids=str)
+def test_sliding_tile_large_windows(dtype, window) -> None:
+    """Windows of up to 65 x 65 cells on a 200 x 260 image (several CTA
+    tiles of 32 x 32 pixels, rows below the last tile row), with and without
+    non-finite pixels."""
+    rng = np.random.default_rng(7)
+    for specials in (False, True):
+        x = _image(rng, (200, 260), dtype, specials=specials)
+        assert_bitwise(E.equalize_histogram_sliding_tile(x, 256, window),
+                       H.equalize_sliding_tile(x, 256, window))
