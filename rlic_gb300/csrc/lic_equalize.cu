@@ -17,8 +17,10 @@
 //   3b. tile interpolation: one CTA per tile builds its histogram in shared
 //       memory, scans it and writes the tile's mapping; each pixel then
 //       blends the mappings of its four nearest tile centres;
-//   3c. sliding tile: each pixel counts the bins <= its own in its window
-//       (reads through L1; neighbouring pixels share the window's lines).
+//   3c. sliding tile: each thread slides one column's window down a run of
+//       rows, keeping the window's histogram in shared memory (2 tw cell
+//       updates per pixel); windows beyond 65535 cells or more than 256
+//       bins count every window cell per pixel instead.
 #include "../../include/rlic_gb300.h"
 #include "lic_equalize.h"
 #include "lic_launch.h"
@@ -516,6 +518,129 @@ sliding_smem_rows_kernel(const T* __restrict__ x, const int32_t* __restrict__ bi
     }
 }
 
+// Sliding windows kept as running histograms.  Each thread owns one output
+// column j and a run of `rows` consecutive output rows, and keeps the
+// histogram of its current window in shared memory: the counts of bins 2m
+// and 2m + 1 packed in word m (16 bits each, so a window holds at most
+// 65535 cells), word m of thread t at s_hist[m * kHistThreads + t] (every
+// lane of a warp in its own bank).  Moving down one row subtracts the
+// window's top row and adds the row below it: 2 tw cells per pixel instead
+// of the th tw cells that a full count reads.  The rank of the pixel's bin
+// is the sum of the words below it (the packed halves add without carry,
+// each half's total being at most the window's cell count) plus the pixel's
+// own word.  Shared-memory atomics do the updates: their results are never
+// read back, so they issue without waiting on one another.  ALL_FINITE:
+// the image has no non-finite pixel, so every cell inside the image counts
+// and the clipped window's area is the valid count.
+constexpr int kHistThreads = 128;
+
+template <typename T, bool ALL_FINITE>
+__device__ __forceinline__ void sliding_hist_run(const T* __restrict__ x,
+                                                 const int32_t* __restrict__ bins, int64_t ny,
+                                                 int64_t nx, int th, int tw, int nbins, int rows,
+                                                 T* __restrict__ out, uint32_t* s_hist) {
+    const int words = (nbins + 1) / 2;
+    const int t = threadIdx.x;
+    uint32_t* hist = s_hist + t;
+    for (int m = 0; m < words; ++m) hist[m * kHistThreads] = 0u;
+    const int64_t j = int64_t(blockIdx.x) * kHistThreads + t;
+    if (j >= nx) return;  // (each thread works on its own words only)
+    const int64_t i0 = int64_t(blockIdx.y) * rows;
+    const int64_t i1 = i0 + rows < ny ? i0 + rows : ny;
+    const int64_t cl = j - tw / 2 < 0 ? 0 : j - tw / 2;
+    const int64_t cr = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
+    int32_t nvalid = 0;
+    // adds (SIGN 1) or removes (SIGN -1) one cell of bin b: word b / 2, half
+    // b % 2.  A non-finite cell (b = -1, only when !ALL_FINITE) adds 0 to
+    // word 0.  No branch: the atomics issue back to back.
+    auto apply = [&](int32_t b, int sign) {
+        uint32_t ub = uint32_t(b), inc;
+        if (ALL_FINITE) {
+            inc = (ub & 1u) * 0xFFFFu + 1u;
+        } else {
+            const bool ok = b >= 0;
+            ub = ok ? ub : 0u;
+            inc = ok ? (ub & 1u) * 0xFFFFu + 1u : 0u;
+            nvalid += ok ? sign : 0;
+        }
+        uint32_t* w = hist + (ub >> 1) * kHistThreads;
+        if (sign > 0) {
+            atomicAdd(w, inc);
+        } else {
+            atomicSub(w, inc);
+        }
+    };
+    // the window's cells of image row r (inside the image) enter it (sign 1)
+    // or leave it (sign -1); the bins are loaded 8 columns at a time before
+    // any is applied, so that 8 loads are in flight
+    auto row_update = [&](int64_t r, int sign) {
+        const int32_t* p = bins + r * nx;
+        int64_t c = cl;
+        for (; c + 8 <= cr; c += 8) {
+            int32_t b[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) b[k] = __ldg(p + c + k);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) apply(b[k], sign);
+        }
+        for (; c < cr; ++c) apply(__ldg(p + c), sign);
+    };
+    // the first window: rows [i0 - th/2, i0 - th/2 + th) inside the image
+    {
+        const int64_t r0 = i0 - th / 2 < 0 ? 0 : i0 - th / 2;
+        const int64_t r1 = i0 - th / 2 + th > ny ? ny : i0 - th / 2 + th;
+        for (int64_t r = r0; r < r1; ++r) row_update(r, 1);
+    }
+    const int64_t c_span = cr - cl;
+    for (int64_t i = i0; i < i1; ++i) {
+        if (i > i0) {
+            const int64_t r_out = i - 1 - th / 2, r_in = i - th / 2 + th - 1;
+            if (r_out >= 0) row_update(r_out, -1);
+            if (r_in < ny) row_update(r_in, 1);
+        }
+        const int64_t k = i * nx + j;
+        const int32_t b = __ldg(bins + k);
+        if (!ALL_FINITE && b < 0) {
+            out[k] = x[k];
+            continue;
+        }
+        const uint32_t hb = uint32_t(b) >> 1;
+        uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        uint32_t m = 0;
+        for (; m + 4 <= hb; m += 4) {
+            a0 += hist[m * kHistThreads];
+            a1 += hist[(m + 1) * kHistThreads];
+            a2 += hist[(m + 2) * kHistThreads];
+            a3 += hist[(m + 3) * kHistThreads];
+        }
+        for (; m < hb; ++m) a0 += hist[m * kHistThreads];
+        const uint32_t acc = a0 + a1 + a2 + a3;
+        const uint32_t own = hist[hb * kHistThreads];
+        const uint32_t below = (acc & 0xFFFFu) + (acc >> 16) + (own & 0xFFFFu) +
+                               ((uint32_t(b) & 1u) ? (own >> 16) : 0u);
+        uint32_t valid = uint32_t(nvalid);
+        if (ALL_FINITE) {  // the window clipped to the image
+            const int64_t r0 = i - th / 2 < 0 ? 0 : i - th / 2;
+            const int64_t r1 = i - th / 2 + th > ny ? ny : i - th / 2 + th;
+            valid = uint32_t((r1 - r0) * c_span);
+        }
+        out[k] = div_rn_(from_count<T>(below), from_count<T>(valid));
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kHistThreads)
+sliding_hist_kernel(const T* __restrict__ x, const int32_t* __restrict__ bins, int64_t ny,
+                    int64_t nx, int th, int tw, int nbins, int rows, const Stats<T>* st,
+                    T* __restrict__ out) {
+    extern __shared__ uint32_t s_hist[];
+    if (st->count == (unsigned long long)(ny * nx)) {
+        sliding_hist_run<T, true>(x, bins, ny, nx, th, tw, nbins, rows, out, s_hist);
+    } else {
+        sliding_hist_run<T, false>(x, bins, ny, nx, th, tw, nbins, rows, out, s_hist);
+    }
+}
+
 unsigned grid_for(int64_t n) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 152 * 8) blocks = 152 * 8;
@@ -589,6 +714,31 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
         const int64_t gy = ny < 1024 ? ny : 1024;
         map_tiles_kernel<T><<<dim3(unsigned((nx + 255) / 256), unsigned(gy)), 256, 0, stream>>>(
             x, bins, ny, nx, ntx, nbins, a0, a1, f, maps, out);
+        count_launch();
+    } else if (nbins <= 256 && th * tw <= 65535) {
+        // running window histograms: one wave of CTAs, each sliding its
+        // 128 columns down one run of rows (the first window of a run costs
+        // th * tw cells, every later one 2 tw), runs of at least 32 rows
+        const size_t smem = size_t((nbins + 1) / 2) * kHistThreads * 4;
+        auto kfn = sliding_hist_kernel<T>;
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+            if (e != cudaSuccess) return e;
+        }
+        int dev = 0, sms = 0, per_sm = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kHistThreads, smem);
+        if (e != cudaSuccess) return e;
+        const int64_t gx = (nx + kHistThreads - 1) / kHistThreads;
+        int64_t gy = int64_t(sms) * (per_sm < 1 ? 1 : per_sm) / gx;
+        const int64_t most = (ny + 31) / 32;
+        gy = gy < 1 ? 1 : (gy > most ? most : gy);
+        const int64_t rows = (ny + gy - 1) / gy;
+        gy = (ny + rows - 1) / rows;
+        kfn<<<dim3(unsigned(gx), unsigned(gy)), kHistThreads, smem, stream>>>(
+            x, bins, ny, nx, int(th), int(tw), nbins, int(rows), st, out);
         count_launch();
     } else {
         const int64_t gy = (ny + 7) / 8;

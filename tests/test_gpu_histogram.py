@@ -118,3 +118,62 @@ def test_sliding_tile_large_windows(dtype, window) -> None:
         x = _image(rng, (200, 260), dtype, specials=specials)
         assert_bitwise(E.equalize_histogram_sliding_tile(x, 256, window),
                        H.equalize_sliding_tile(x, 256, window))
+
+
+def _sliding_by_box_sums(x, nbins, window):
+    """The sliding-tile definition of oracle/histogram.py evaluated with box
+    sums of indicator images (one per bin level): the same counts, so the
+    same roundings, at a cost independent of the window size."""
+    th, tw = window
+    b = H.bins(x, nbins)
+    ny, nx = x.shape
+
+    def box(ind):
+        c = np.zeros((ny + 1, nx + 1), dtype=np.int64)
+        c[1:, 1:] = np.cumsum(np.cumsum(ind.astype(np.int64), 0), 1)
+        i = np.arange(ny)[:, None]
+        j = np.arange(nx)[None, :]
+        r0, r1 = np.clip(i - th // 2, 0, ny), np.clip(i - th // 2 + th, 0, ny)
+        c0, c1 = np.clip(j - tw // 2, 0, nx), np.clip(j - tw // 2 + tw, 0, nx)
+        return c[r1, c1] - c[r0, c1] - c[r1, c0] + c[r0, c0]
+
+    valid = box(b >= 0)
+    below = np.zeros_like(valid)
+    for k in range(nbins):
+        below = np.where(b == k, box((b >= 0) & (b <= k)), below)
+    out = x.copy()
+    fin = b >= 0
+    out[fin] = (below[fin].astype(x.dtype) / valid[fin].astype(x.dtype)).astype(x.dtype)
+    return out
+
+
+def test_box_sum_restatement_matches_definition() -> None:
+    rng = np.random.default_rng(5)
+    x = _image(rng, (40, 50), np.float32)
+    for nbins, window in ((2, (9, 13)), (3, (64, 7))):
+        assert_bitwise(_sliding_by_box_sums(x, nbins, window),
+                       H.equalize_sliding_tile(x, nbins, window))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("nbins, window", [(2, (255, 257)), (1, (255, 257)), (2, (257, 257))],
+                         ids=str)
+def test_sliding_tile_histogram_limits(dtype, nbins, window) -> None:
+    """Windows of 65535 cells, the most the running window histograms hold
+    (with one or two bins a bin's count reaches the 16-bit limit), and one
+    of 66049 cells, which counts every window cell per pixel instead, on a
+    300 x 300 image with and without non-finite pixels."""
+    rng = np.random.default_rng(11)
+    for specials in (False, True):
+        x = _image(rng, (300, 300), dtype, specials=specials)
+        assert_bitwise(E.equalize_histogram_sliding_tile(x, nbins, window),
+                       _sliding_by_box_sums(x, nbins, window))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_sliding_tile_many_bins(dtype) -> None:
+    """More than 256 bins: counted per window cell."""
+    rng = np.random.default_rng(12)
+    x = _image(rng, (60, 70), dtype)
+    assert_bitwise(E.equalize_histogram_sliding_tile(x, 300, (9, 9)),
+                   H.equalize_sliding_tile(x, 300, (9, 9)))
