@@ -85,8 +85,7 @@ RLIC_API const char *rlic_last_error(void);
  * ny x nx elements of `elem_bytes` (4 or 8) bytes, a kernel of klen taps,
  * `iterations` passes and the given flags: the packed (u, v) field, for two
  * or more iterations one ping-pong texture buffer, (unless
- * RLIC_FLAG_NO_PATH_CACHE) the path cache for two or more iterations or for
- * an image small enough to trace as split halves (rlic_set_split_pixels), a
+ * RLIC_FLAG_NO_PATH_CACHE) the path cache for two or more iterations, a
  * copy of the kernel and a flag that records whether the field holds a NaN
  * sample.
  * 0 on invalid arguments.
@@ -424,17 +423,20 @@ RLIC_API int rlic_replay_f64(const double *tex_in, const void *codes, int64_t ny
 #define RLIC_REPLAY_STAGED 2
 RLIC_API int rlic_set_replay_mode(int mode, int stage_rows);
 /*
- * Images of at most max_pixels pixels (default 0: none) trace their first
- * pass as split halves, one thread per half-streamline, recording the path
- * cache, and then replay it: on images too small to fill the GPU this
- * doubles the parallelism of the streamline arithmetic, but on every size
- * measured the extra replay cost more than that gained.  Bit-identical to
- * the single traced pass; 0 turns it off.  The workspace of such calls
- * holds the path cache even for one iteration (rlic_workspace_bytes counts
- * it under the setting in force), so change the setting only between calls
- * that size their workspace again.  RLIC_FLAG_NO_PATH_CACHE calls never
- * split.  Affects calls made after it on any thread.  No counterpart in the
- * reference (a tuning knob of this implementation).
+ * Images of at most max_pixels pixels (default: 2^18 for float64 images,
+ * 2^16 for float32) trace every traced pass with each pixel's two
+ * half-streamlines on two threads of one warp: the forward thread
+ * accumulates the centre tap and its own samples, the backward thread hands
+ * its samples over through shared memory, and the forward thread adds them
+ * in the reference's order.  On images too small to fill the GPU this
+ * doubles the threads that run the serial streamline arithmetic.
+ * Bit-identical to the one-thread-per-pixel pass; 0 turns it off and -1
+ * restores the defaults.  Launches that do not fit the form (kernels of
+ * fewer than 3 taps, CTA shapes of other than a multiple of 16 pixels up to
+ * 64, backward samples beyond 96 KiB of shared memory, images of 2^31
+ * pixels or more) keep one thread per pixel.  Affects calls made after it on
+ * any thread.  No counterpart in the reference (a tuning knob of this
+ * implementation).
  */
 RLIC_API int rlic_set_split_pixels(int64_t max_pixels);
 /*
@@ -449,9 +451,10 @@ RLIC_API int rlic_stage_timeouts(void);
  * pixels (block_x * block_y threads, at most 256; block_x a multiple of 32
  * or a divisor of 32).  Affects calls made after it on any thread.  Until
  * it is called, traced passes use 16 x 8 (8 x 8 for images of at most 2^19
- * pixels: more CTAs even the SMs' load when an image has few tiles) and
- * replays through L1 use 64 x 4; once called, every kernel uses the shape
- * given.
+ * pixels, 4 x 4 for paired passes over images of at most 2^17 pixels: more
+ * CTAs even the SMs' load when an image has few tiles) and replays through
+ * L1 use 64 x 4; once called, every kernel uses the shape given.  (0, 0)
+ * restores those defaults.
  */
 RLIC_API int rlic_set_block_shape(int block_x, int block_y);
 

@@ -205,7 +205,8 @@ def set_block_shape(block_x: int, block_y: int) -> None:
 
 
 def set_split_pixels(max_pixels: int) -> None:
-    """Images of at most max_pixels trace their first pass as split halves."""
+    """Images of at most max_pixels trace each pixel's two half-streamlines on
+    two threads (0: never; -1: the library's default threshold)."""
     check(lib().rlic_set_split_pixels(max_pixels))
 
 

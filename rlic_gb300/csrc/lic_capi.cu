@@ -162,13 +162,22 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 #define RLIC_HOST_CHUNKS 8
 #endif
 
-// Off by default: on every size measured (128^2 to 1024^2, float32 and
-// float64, 1 and 5 passes) the split first pass and its replay were slower
-// than one fused traced pass (256^2 float64, one pass: 0.204 against
-// 0.160 ms; float32: 0.060 against 0.032 ms).
-#ifndef RLIC_SPLIT_PIXELS_DEFAULT
-#define RLIC_SPLIT_PIXELS_DEFAULT 0
-#endif
+// Images of at most this many pixels trace their passes with each pixel's
+// two half-streamlines on two threads (lic_pass_paired_kernel) unless
+// rlic_set_split_pixels chose a threshold.  Measured on GB300, calls of one
+// pass on device memory (ms): float64 256^2, 65 taps 0.103 (4 x 4-pixel
+// tiles) against 0.114-0.117 with one thread per pixel, 512^2 0.347 against
+// 0.374; float32 256^2 0.028 against 0.030, 512^2 0.064 against 0.058.  The
+// paired form spends about 12% more FP64 instructions (the forward thread
+// adds the backward samples after its own), and the float32 pass is bound
+// by instruction issue, so it pays only where the image alone cannot fill
+// the GPU with threads.
+constexpr int64_t kPairedPixelsF64 = int64_t(1) << 18;
+constexpr int64_t kPairedPixelsF32 = int64_t(1) << 16;
+// Paired passes over images of at most this many pixels use 4 x 4-pixel
+// tiles (one warp per CTA: with about 27 CTAs per SM the SMs' loads differ
+// by one CTA in 27, against one in 7 with 8 x 8 tiles on a 256^2 image).
+constexpr int64_t kPairedSmallTilePixels = int64_t(1) << 17;
 
 // A non-blocking stream per device for the uploads of host-memory calls, at
 // the greatest priority: the block scheduler then gives the upload kernels
@@ -234,13 +243,23 @@ LaunchConfig launch_config() { return LaunchConfig{g_block_x.load(), g_block_y.l
 std::atomic<bool> g_block_custom{false};
 constexpr int64_t kSmallImagePixels = int64_t(1) << 19;
 
-LaunchConfig launch_config_for(int64_t ny, int64_t nx) {
+int64_t split_pixels(size_t elem);
+
+// Launch shape of the traced passes of an ny x nx image of `elem`-byte
+// elements (4 or 8) and a kernel of klen taps.
+LaunchConfig launch_config_for(int64_t ny, int64_t nx, size_t elem, int64_t klen) {
     LaunchConfig lc = launch_config();
     if (!g_block_custom.load()) {
         const bool small = ny * nx <= kSmallImagePixels;
         lc.block_x = small ? 8 : 16;
         lc.block_y = 8;
+        if (ny * nx <= split_pixels(elem) && ny * nx <= kPairedSmallTilePixels &&
+            rlic::paired_launch_fits(ny * nx, 4, 4, klen, elem)) {
+            lc.block_x = 4;
+            lc.block_y = 4;
+        }
     }
+    lc.paired = ny * nx <= split_pixels(elem);
     return lc;
 }
 
@@ -307,17 +326,17 @@ Shape make_shape(int64_t ny, int64_t nx, const int bnd[4]) {
     return sh;
 }
 
-// Images of at most this many pixels trace their first pass as split
-// halves (lic_record_halves_kernel, one thread per half-streamline) followed
-// by a replay, which doubles the parallelism of the streamline arithmetic
-// where an image's tiles alone cannot fill the GPU (rlic_set_split_pixels;
-// off by default, see RLIC_SPLIT_PIXELS_DEFAULT).
-std::atomic<int64_t> g_split_pixels{RLIC_SPLIT_PIXELS_DEFAULT};
+// Images of at most this many pixels trace each pass's two half-streamlines
+// of a pixel on two threads of one warp (lic_pass_paired_kernel), which
+// doubles the threads running the serial streamline arithmetic where an
+// image's tiles alone cannot fill the GPU (rlic_set_split_pixels).
+// (-1: the per-dtype defaults kPairedPixelsF32 / kPairedPixelsF64)
+std::atomic<int64_t> g_split_pixels{-1};
 
-int64_t split_pixels() { return g_split_pixels.load(); }
-
-bool use_split(int64_t ny, int64_t nx, int64_t klen, unsigned flags) {
-    return klen > 1 && !(flags & RLIC_FLAG_NO_PATH_CACHE) && ny * nx <= split_pixels();
+int64_t split_pixels(size_t elem) {
+    const int64_t v = g_split_pixels.load();
+    if (v >= 0) return v;
+    return elem == sizeof(double) ? kPairedPixelsF64 : kPairedPixelsF32;
 }
 
 bool use_path_cache(int64_t iterations, int64_t klen, unsigned flags) {
@@ -342,8 +361,7 @@ WorkspaceLayout workspace_layout(int64_t ny, int64_t nx, int64_t klen, int64_t i
     w.tmp = off;
     if (iterations >= 2) off += align_up(n * s);
     w.codes = off;
-    if (use_path_cache(iterations, klen, flags) || use_split(ny, nx, klen, flags))
-        off += align_up(code_bytes(ny, nx, klen));
+    if (use_path_cache(iterations, klen, flags)) off += align_up(code_bytes(ny, nx, klen));
     w.kernel = off;
     off += align_up(size_t(klen) * s);
     w.nan = off;  // flag: the packed field holds a NaN sample
@@ -376,10 +394,9 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
     void* uv = ws + wl.uv;
     T* tmp = reinterpret_cast<T*>(ws + wl.tmp);
     uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
-    const bool split = use_split(ny, nx, klen, flags);
-    const bool cache = use_path_cache(iterations, klen, flags) || split;
+    const bool cache = use_path_cache(iterations, klen, flags);
     const Shape sh = make_shape(ny, nx, bnd);
-    LaunchConfig lc = launch_config_for(ny, nx);
+    LaunchConfig lc = launch_config_for(ny, nx, sizeof(T), klen);
     if (!uv_ready) {
         unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
         RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
@@ -393,12 +410,7 @@ int run_device(const T* texture, const T* u, const T* v, int64_t ny, int64_t nx,
             before_last();
             if (final_out) dst = final_out;
         }
-        if (it == 0 && split) {
-            RLIC_CUDA_TRY(rlic::launch_record_halves(var, texture, uv, int(klen), sh, lc, codes,
-                                                     stream));
-            RLIC_CUDA_TRY(replay_pass(var.fma, src, codes, kernel, int(klen), sh, lc, dst,
-                                      stream));
-        } else if (it == 0 || !cache) {
+        if (it == 0 || !cache) {
             RLIC_CUDA_TRY(rlic::launch_pass(var, cache ? rlic::kPassSampleRecord : rlic::kPassSample,
                                             src, uv, kernel, int(klen), sh, lc, dst, codes,
                                             stream));
@@ -538,12 +550,9 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
         RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
         unsigned char* uvb = ws + wl.uv;
-        // small images (one upload chunk) trace their first pass as split
-        // halves, then replay it
-        const bool split = use_split(ny, nx, klen, flags) && nchunks == 1;
-        const bool cache = use_path_cache(iterations, klen, flags) || split;
+        const bool cache = use_path_cache(iterations, klen, flags);
         const Shape sh = make_shape(ny, nx, bnd);
-        const LaunchConfig lc = launch_config_for(ny, nx);
+        const LaunchConfig lc = launch_config_for(ny, nx, sizeof(T), klen);
         const int64_t tiles_x = (nx + lc.block_x - 1) / lc.block_x;
         const int64_t tile_rows = (ny + lc.block_y - 1) / lc.block_y;
         // arrival position after which each tile row has its rows and halo
@@ -614,15 +623,8 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 // a NaN in a chunk that has not arrived yet cannot be reached
                 // from these tile rows, so the flag's value now suffices
                 part.field_nan = nan_flag;
-                if (split) {
-                    RLIC_CUDA_TRY(rlic::launch_record_halves(var, d_tex, uvb, int(klen), sh, part,
-                                                             codes, stream));
-                    RLIC_CUDA_TRY(replay_pass(var.fma, d_tex, codes, d_kernel, int(klen), sh,
-                                              part, dst_of(0), stream));
-                } else {
-                    RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen),
-                                                    sh, part, dst_of(0), codes, stream));
-                }
+                RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen), sh,
+                                                part, dst_of(0), codes, stream));
                 tr = tr_end;
             }
         }
@@ -764,7 +766,7 @@ int sweep_impl(const T* tex_in, const void* uv, int64_t ny, int64_t nx, const T*
     if (codes && reinterpret_cast<uintptr_t>(codes) % 4 != 0)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "codes must be 4-byte aligned");
     const Variant var = make_variant(flags, uv_mode);
-    LaunchConfig lc = launch_config_for(ny, nx);
+    LaunchConfig lc = launch_config_for(ny, nx, sizeof(T), klen);
     if (flags & RLIC_FLAG_FIELD_NAN_FREE) {
         cudaError_t e = cudaSuccess;
         lc.field_nan = rlic::zero_flag(&e);
@@ -874,7 +876,7 @@ int convolve_lowp_impl(const T* texture, const T* u, const T* v, int64_t ny, int
     }
     auto body = [&]() -> int {
         const Shape sh = make_shape(ny, nx, bnd);
-        const LaunchConfig lc = launch_config_for(ny, nx);
+        const LaunchConfig lc = launch_config_for(ny, nx, sizeof(T), klen);
         void* uv = ws + wl.uv;
         uint32_t* codes = reinterpret_cast<uint32_t*>(ws + wl.codes);
         float* w32 = reinterpret_cast<float*>(ws + wl.w32);
@@ -1542,7 +1544,7 @@ int rlic_set_replay_mode(int mode, int stage_rows) {
 
 int rlic_set_split_pixels(int64_t max_pixels) {
     g_last_error.clear();
-    if (max_pixels < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "max_pixels must be >= 0");
+    if (max_pixels < -1) return fail(RLIC_ERR_INVALID_ARGUMENT, "max_pixels must be >= -1");
     g_split_pixels.store(max_pixels);
     return RLIC_OK;
 }
@@ -1554,6 +1556,13 @@ int rlic_stage_timeouts(void) {
 }
 
 int rlic_set_block_shape(int block_x, int block_y) {
+    g_last_error.clear();
+    if (block_x == 0 && block_y == 0) {  // the defaults
+        g_block_x.store(64);
+        g_block_y.store(4);
+        g_block_custom.store(false);
+        return RLIC_OK;
+    }
     if (block_x <= 0 || block_y <= 0 || block_x * block_y > 256)
         return fail(RLIC_ERR_INVALID_ARGUMENT, "block shape must have 1..256 threads");
     g_block_x.store(block_x);

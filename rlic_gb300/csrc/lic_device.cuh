@@ -668,20 +668,34 @@ struct TraceState {
     T lu, lv;  // previous sample in polarization mode, starting at (0, 0)
     int last;  // axis of the last move (kLastNone before the first)
     I cell, i, j;
+    bool back;  // direction chosen at run time (kDirRuntime): backward
 };
+
+// Direction of a half-trace: forward, backward, or chosen per thread at run
+// time (TraceState::back), for kernels whose lanes trace both halves.
+constexpr int kDirForward = 0, kDirBackward = 1, kDirRuntime = 2;
+
+// -x when n is set, x otherwise: a sign-bit edit (integer instruction).
+__device__ __forceinline__ float neg_if(float x, bool n) {
+    return __uint_as_float(__float_as_uint(x) ^ (n ? 0x80000000u : 0u));
+}
+__device__ __forceinline__ double neg_if(double x, bool n) {
+    return from_bits(bits_of(x) ^ (uint64_t(n) << 63));
+}
 
 // One step of convole_single_pixel (src/lib.rs:331-361): read u and v at the
 // current cell, stop on NaN (returns false), flip the sample against the
 // previous one in polarization mode (the dot product is two separately
 // rounded products and a rounded sum, src/lib.rs:341), negate it for the
 // backward trace, advance, then accumulate weight * texture at the new cell.
-// `code` receives the step code.
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
+// `code` receives the step code; `x_out`, when given, the texture sample.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int DIR, bool EDGE,
           bool SAMPLE, typename I, bool NAN_CHECK = true, bool NC = true>
 __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
                                            const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
-                                           const T* __restrict__ tex, uint32_t& code) {
+                                           const T* __restrict__ tex, uint32_t& code,
+                                           T* x_out = nullptr) {
     const auto p = ld_in<NC>(uv + st.cell);
     T pu = p.x, pv = p.y;
     // (NAN_CHECK false: the caller knows the field holds no NaN sample)
@@ -701,13 +715,20 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
         st.lu = pu;
         st.lv = pv;
     }
-    if constexpr (BACKWARD) {
+    if constexpr (DIR == kDirBackward) {
         pu = neg_(pu);
         pv = neg_(pv);
+    } else if constexpr (DIR == kDirRuntime) {
+        pu = neg_if(pu, st.back);
+        pv = neg_if(pv, st.back);
     }
     code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, st.last,
                                              g);
-    if constexpr (SAMPLE) acc = accumulate<T, FMA>(w, ld_in<NC>(tex + st.cell), acc);
+    if constexpr (SAMPLE) {
+        const T x = ld_in<NC>(tex + st.cell);
+        acc = accumulate<T, FMA>(w, x, acc);
+        if (x_out) *x_out = x;
+    }
     return true;
 }
 
@@ -720,7 +741,7 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
 // Steps run in groups of 8, one 32-bit word of step codes per group; with
 // RECORD the word is stored at words[group * stride].  A trace that stops on
 // NaN stores the stop code in place of its step and nothing after it.
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, bool EDGE,
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int DIR, bool EDGE,
           bool SAMPLE, bool RECORD, typename I, bool NAN_CHECK = true, bool NC = true>
 __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
@@ -735,6 +756,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
     st.cell = i * g.nx + j;
     st.i = i;
     st.j = j;
+    st.back = DIR == kDirBackward;
     const int full = count >> 3;
     for (int q = 0; q < full; ++q) {
         const T* wq = w + 8 * q;
@@ -742,7 +764,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK, NC>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, DIR, EDGE, SAMPLE, I, NAN_CHECK, NC>(
                     st, acc, SAMPLE ? wq[b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                 return;
@@ -756,7 +778,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
         uint32_t word = 0;
         for (int b = 0; b < rest; ++b) {
             uint32_t code = 0;
-            if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, EDGE, SAMPLE, I, NAN_CHECK, NC>(
+            if (!trace_step<T, FMA, BRANCHLESS, POL, DIR, EDGE, SAMPLE, I, NAN_CHECK, NC>(
                     st, acc, SAMPLE ? w[8 * full + b] : T(0), g, uv, tex, code)) {
                 if constexpr (RECORD) words[size_t(full) * stride] = word | (kStop << (4 * b));
                 return;
@@ -769,7 +791,7 @@ __device__ __forceinline__ void trace_half(T& acc, I i, I j, const Geometry<I>& 
 
 // The same walk for path parity checks: reports the cell reached by every
 // step to `rec(s, cell)`.
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool BACKWARD, typename I, typename Rec>
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int DIR, typename I, typename Rec>
 __device__ __forceinline__ void walk_half(I i, I j, const Geometry<I>& g,
                                           const typename Vec2<T>::type* __restrict__ uv,
                                           int count, Rec rec) {
@@ -782,10 +804,11 @@ __device__ __forceinline__ void walk_half(I i, I j, const Geometry<I>& g,
     st.cell = i * g.nx + j;
     st.i = i;
     st.j = j;
+    st.back = DIR == kDirBackward;
     T acc = T(0);
     for (int s = 0; s < count; ++s) {
         uint32_t code = 0;
-        if (!trace_step<T, FMA, BRANCHLESS, POL, BACKWARD, true, false>(
+        if (!trace_step<T, FMA, BRANCHLESS, POL, DIR, true, false>(
                 st, acc, T(0), g, uv, static_cast<const T*>(nullptr), code))
             return;
         rec(s, st.cell);

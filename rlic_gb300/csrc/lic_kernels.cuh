@@ -57,6 +57,19 @@ namespace rlic {
 
 template <typename T, typename I> struct PassMinBlocks { static constexpr int value = 1; };
 
+// The paired pass (two threads per pixel, CTAs of at most kPairedMaxThreads
+// threads): the float64 form waits on FP64 results and wants every pixel of
+// a small image resident at once; 7 CTAs of 128 threads per SM (72
+// registers) hold a 256^2 image's 131072 threads in one wave.
+constexpr int kPairedMaxThreads = 128;
+#ifndef RLIC_PAIRED_MIN_BLOCKS_F64
+#define RLIC_PAIRED_MIN_BLOCKS_F64 7
+#endif
+template <typename T> struct PairedMinBlocks { static constexpr int value = 1; };
+template <> struct PairedMinBlocks<double> {
+    static constexpr int value = RLIC_PAIRED_MIN_BLOCKS_F64;
+};
+
 template <typename T, typename I> struct GatherMinBlocks { static constexpr int value = 4; };
 template <> struct GatherMinBlocks<float, int32_t> {
     static constexpr int value = RLIC_GATHER_MIN_BLOCKS;
@@ -145,9 +158,9 @@ __device__ __forceinline__ T convolve_pixel(I i, I j, const Geometry<I>& g,
     if constexpr (SAMPLE) acc = accumulate<T, FMA>(wmid, ld_in<NC>(tex + p), T(0));
     uint32_t* words_f = RECORD ? codes + p : nullptr;
     uint32_t* words_b = RECORD ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : nullptr;
-    trace_half<T, FMA, BRANCHLESS, POL, false, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
+    trace_half<T, FMA, BRANCHLESS, POL, kDirForward, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
         acc, i, j, g, uv, tex, wf, nf, words_f, cl.npix);
-    trace_half<T, FMA, BRANCHLESS, POL, true, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
+    trace_half<T, FMA, BRANCHLESS, POL, kDirBackward, EDGE, SAMPLE, RECORD, I, NAN_CHECK, NC>(
         acc, i, j, g, uv, tex, wb, kmid, words_b, cl.npix);
     return acc;
 }
@@ -196,47 +209,122 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
     if constexpr (MODE != kRecordOnly) tex_out[i * g.nx + j] = acc;
 }
 
-// Records the step codes of one half of every pixel's streamline, without
-// sampling: CTA 2 t traces the forward halves of tile t, CTA 2 t + 1 the
-// backward halves.  On images too small to fill the GPU, splitting the two
-// halves over two threads doubles the parallelism of the streamline
-// arithmetic (the trace's work is a serial chain per half); a replay then
-// accumulates every pixel in the reference's order (centre, forward taps
-// ascending, backward taps descending), so the output is the traced pass's.
-template <typename T, bool FMA, bool BRANCHLESS, bool POL, typename I>
-__global__ void __launch_bounds__(256, (PassMinBlocks<T, I>::value))
-lic_record_halves_kernel(const typename Vec2<T>::type* __restrict__ uv, int klen, Geometry<I> g,
-                         TileGrid<I> tg, uint32_t* __restrict__ codes, CodeLayout cl,
-                         const unsigned* __restrict__ field_nan) {
+// One half of a pixel's streamline for the paired pass below: the direction
+// is the thread's (st.back); every step's texture sample is accumulated into
+// `acc` with this half's weights `w` and, on backward threads, also stored
+// at sink[s * sink_stride] for step s.  Records step codes like trace_half.
+// Returns the number of steps sampled (count, or the step that met a NaN
+// sample and stopped the trace).
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, bool RECORD, typename I,
+          bool NAN_CHECK>
+__device__ __forceinline__ int trace_paired_half(T& acc, I i, I j, bool back,
+                                                 const Geometry<I>& g,
+                                                 const typename Vec2<T>::type* __restrict__ uv,
+                                                 const T* __restrict__ tex, const T* w,
+                                                 int count, uint32_t* __restrict__ words,
+                                                 size_t stride, T* sink, int sink_stride) {
+    TraceState<T, I> st;
+    st.last = kLastNone;
+    st.fx = T(0.5);
+    st.fy = T(0.5);
+    st.lu = T(0);
+    st.lv = T(0);
+    st.cell = i * g.nx + j;
+    st.i = i;
+    st.j = j;
+    st.back = back;
+    for (int q = 0; 8 * q < count; ++q) {
+        const int n = count - 8 * q < 8 ? count - 8 * q : 8;
+        const T* wq = w + 8 * q;
+        uint32_t word = 0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            if (b < n) {
+                uint32_t code = 0;
+                T x;
+                if (!trace_step<T, FMA, BRANCHLESS, POL, kDirRuntime, EDGE, true, I, NAN_CHECK>(
+                        st, acc, wq[b], g, uv, tex, code, &x)) {
+                    if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
+                    return 8 * q + b;
+                }
+                if (back) sink[(8 * q + b) * sink_stride] = x;
+                word |= code << (4 * b);
+            }
+        }
+        if constexpr (RECORD) words[size_t(q) * stride] = word;
+    }
+    return count;
+}
+
+// One convolution pass with each pixel's two half-streamlines traced by two
+// threads of one warp: lanes 0-15 trace the forward halves of 16 pixels,
+// lanes 16-31 the backward halves of the same pixels.  On images whose
+// tiles cannot fill the GPU this doubles the threads that run the serial
+// streamline arithmetic (each thread's chain of steps is half as long).  The
+// output keeps the reference's accumulation order (centre tap, forward taps
+// ascending, backward taps descending, src/lib.rs:376-403): the forward
+// thread accumulates the centre and its own samples as it steps, while the
+// backward thread stores its samples in shared memory; the forward thread
+// then adds them in step order.  A CTA of 2 * bx * by threads owns a tile of
+// bx x by pixels (bx * by a multiple of 16, at most 64); pixel slot
+// 16 * warp + (lane & 15) is tile row slot / bx, column slot % bx.
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
+__global__ void __launch_bounds__(kPairedMaxThreads, (PairedMinBlocks<T>::value))
+lic_pass_paired_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __restrict__ uv,
+                       const T* __restrict__ kernel, int klen, Geometry<I> g, TileGrid<I> tg,
+                       T* __restrict__ tex_out, uint32_t* __restrict__ codes, CodeLayout cl,
+                       const unsigned* __restrict__ field_nan) {
+    static_assert(MODE != kRecordOnly, "the paired pass samples the texture");
+    constexpr bool RECORD = MODE == kSampleRecord;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* wsm = reinterpret_cast<T*>(smem_raw);
     const int kmid = klen / 2;
     const int nf = klen - kmid - 1;
-    const I tile = tg.tile_base + I(blockIdx.x >> 1);
-    const bool backward = (blockIdx.x & 1u) != 0;
+    const int nf_pad = (nf + 7) & ~7;
+    const int nb_pad = (kmid + 7) & ~7;
+    const int npx = tg.bx * tg.by;
+    T* samples = wsm + nf_pad + nb_pad;  // [kmid][npx]: backward samples by step
+    load_step_weights(wsm, kernel, klen, nf_pad);
+    __syncthreads();
+    const T wmid = __ldg(kernel + kmid);
+    const I tile = tg.tile_base + I(blockIdx.x);
     const I ti = tile / tg.tiles_x;
     const I tj = tile - ti * tg.tiles_x;
-    const I i = ti * tg.by + I(threadIdx.y);
-    const I j = tj * tg.bx + I(threadIdx.x);
+    const int lane = int(threadIdx.x) & 31;
+    const bool back = lane >= 16;
+    const int slot = (int(threadIdx.x) >> 5) * 16 + (lane & 15);
+    const int r = slot / tg.bx;
+    const I i = ti * tg.by + I(r);
+    const I j = tj * tg.bx + I(slot - r * tg.bx);
     const bool interior = tile_is_interior(ti, tj, tg, g);
-    if (!interior && (i >= g.ny || j >= g.nx)) return;
+    const bool valid = interior || (i < g.ny && j < g.nx);
     const bool nan_free = field_nan != nullptr && __ldg(field_nan) == 0u;
-    const I p = i * g.nx + j;
-    uint32_t* words = backward ? codes + size_t(cl.words_f) * size_t(cl.npix) + p : codes + p;
-    const int count = backward ? kmid : nf;
+    const I p = valid ? i * g.nx + j : I(0);
     T acc = T(0);
-#define RLIC_HALF(BACK, EDGE, CHECK)                                                        \
-    trace_half<T, FMA, BRANCHLESS, POL, BACK, EDGE, false, true, I, CHECK>(                  \
-        acc, i, j, g, uv, static_cast<const T*>(nullptr), static_cast<const T*>(nullptr),  \
-        count, words, cl.npix)
-    if (backward) {
-        if (interior && nan_free) RLIC_HALF(true, false, false);
-        else if (interior) RLIC_HALF(true, false, true);
-        else RLIC_HALF(true, true, true);
-    } else {
-        if (interior && nan_free) RLIC_HALF(false, false, false);
-        else if (interior) RLIC_HALF(false, false, true);
-        else RLIC_HALF(false, true, true);
+    int sampled = 0;
+    if (valid) {
+        acc = accumulate<T, FMA>(wmid, __ldg(tex_in + p), T(0));
+        uint32_t* words =
+            RECORD ? codes + (back ? size_t(cl.words_f) * size_t(cl.npix) : size_t(0)) + p
+                   : nullptr;
+        const T* w = back ? wsm + nf_pad : wsm;
+        const int count = back ? kmid : nf;
+        T* sink = samples + slot;
+#define RLIC_PAIRED(EDGE, CHECK)                                                          \
+    trace_paired_half<T, FMA, BRANCHLESS, POL, EDGE, RECORD, I, CHECK>(                   \
+        acc, i, j, back, g, uv, tex_in, w, count, words, size_t(cl.npix), sink, npx)
+        if (interior && nan_free) sampled = RLIC_PAIRED(false, false);
+        else if (interior) sampled = RLIC_PAIRED(false, true);
+        else sampled = RLIC_PAIRED(true, true);
+#undef RLIC_PAIRED
     }
-#undef RLIC_HALF
+    __syncwarp();
+    // the backward partner's sample count (every lane takes part in the shuffle)
+    const int nback = __shfl_sync(0xffffffffu, sampled, (lane & 15) + 16);
+    if (!valid || back) return;
+    const T* wb = wsm + nf_pad;
+    for (int s = 0; s < nback; ++s) acc = accumulate<T, FMA>(wb[s], samples[s * npx + slot], acc);
+    tex_out[p] = acc;
 }
 
 // Replays `count` recorded steps of one half from pixel p.  A word holds 8
@@ -346,9 +434,9 @@ __global__ void trace_cells_kernel(const typename Vec2<T>::type* __restrict__ uv
     if (lin < 0 || lin >= g.ny * g.nx) return;  // invalid pixel: row stays -1
     const int64_t i = lin / g.nx;
     const int64_t j = lin - i * g.nx;
-    walk_half<T, FMA, BRANCHLESS, POL, false>(i, j, g, uv, nf,
+    walk_half<T, FMA, BRANCHLESS, POL, kDirForward>(i, j, g, uv, nf,
                                               [dst](int s, int64_t c) { dst[s] = c; });
-    walk_half<T, FMA, BRANCHLESS, POL, true>(i, j, g, uv, kmid,
+    walk_half<T, FMA, BRANCHLESS, POL, kDirBackward>(i, j, g, uv, kmid,
                                              [dst, nf](int s, int64_t c) { dst[nf + s] = c; });
 }
 
@@ -778,6 +866,62 @@ cudaError_t launch_pack_t(const T* u, const T* v, void* uv, int64_t n, cudaStrea
     return cudaGetLastError();
 }
 
+// The paired pass's shared memory holds the step weights, then kmid
+// backward samples of each of the tile's pixels (paired_smem_bytes in
+// lic_launch.h); paired_launch_fits says when a launch takes that form.
+static_assert(kPairedMaxThreads == kPairedMaxThreadsHost, "paired CTA limit");
+
+inline bool paired_fits(const Shape& sh, const LaunchConfig& lc, int klen, size_t elem) {
+    return paired_launch_fits(sh.ny * sh.nx, lc.block_x, lc.block_y, klen, elem);
+}
+
+template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE>
+cudaError_t launch_paired_t(const T* tex_in, const void* uv, const T* kernel, int klen,
+                            const Shape& sh, const LaunchConfig& lc, T* tex_out, uint32_t* codes,
+                            cudaStream_t stream) {
+    const auto g = make_geometry<int32_t>(sh);
+    const auto tg = make_tiles<int32_t>(sh, lc, klen);
+    const auto cl = make_code_layout(sh, klen);
+    const int npx = lc.block_x * lc.block_y;
+    const size_t smem = paired_smem_bytes(klen, npx, sizeof(T));
+    auto kfn = lic_pass_paired_kernel<T, FMA, BRANCHLESS, POL, MODE, int32_t>;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    const int64_t count = lc.tile_count ? lc.tile_count : int64_t(tg.ntiles) - lc.tile_begin;
+    if (count <= 0) return cudaSuccess;
+    kfn<<<unsigned(count), unsigned(2 * npx), smem, stream>>>(
+        tex_in, static_cast<const typename Vec2<T>::type*>(uv), kernel, klen, g, tg, tex_out,
+        codes, cl, lc.field_nan);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <typename T, int MODE>
+cudaError_t launch_paired_m(const Variant& var, const T* tex_in, const void* uv, const T* kernel,
+                            int klen, const Shape& sh, const LaunchConfig& lc, T* tex_out,
+                            uint32_t* codes, cudaStream_t stream) {
+    const int code = (var.fma ? 4 : 0) | (var.branchless ? 2 : 0) | (var.pol ? 1 : 0);
+#define RLIC_PAIRED_CASE(C, F, B, P)                                                        \
+    case C:                                                                                 \
+        return launch_paired_t<T, F, B, P, MODE>(tex_in, uv, kernel, klen, sh, lc, tex_out, \
+                                                 codes, stream);
+    switch (code) {
+        RLIC_PAIRED_CASE(0, false, false, false)
+        RLIC_PAIRED_CASE(1, false, false, true)
+        RLIC_PAIRED_CASE(2, false, true, false)
+        RLIC_PAIRED_CASE(3, false, true, true)
+        RLIC_PAIRED_CASE(4, true, false, false)
+        RLIC_PAIRED_CASE(5, true, false, true)
+        RLIC_PAIRED_CASE(6, true, true, false)
+        RLIC_PAIRED_CASE(7, true, true, true)
+    }
+#undef RLIC_PAIRED_CASE
+    return cudaErrorInvalidValue;
+}
+
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, int MODE, typename I>
 cudaError_t launch_pass_t(const T* tex_in, const void* uv, const T* kernel, int klen,
                           const Shape& sh, const LaunchConfig& lc, T* tex_out, uint32_t* codes,
@@ -829,6 +973,13 @@ template <typename T, typename I>
 cudaError_t launch_pass_i(const Variant& var, int mode, const T* tex_in, const void* uv,
                           const T* kernel, int klen, const Shape& sh, const LaunchConfig& lc,
                           T* tex_out, uint32_t* codes, cudaStream_t stream) {
+    if (lc.paired && mode != kRecordOnly && paired_fits(sh, lc, klen, sizeof(T))) {
+        return mode == kSample
+                   ? launch_paired_m<T, kSample>(var, tex_in, uv, kernel, klen, sh, lc, tex_out,
+                                                 codes, stream)
+                   : launch_paired_m<T, kSampleRecord>(var, tex_in, uv, kernel, klen, sh, lc,
+                                                       tex_out, codes, stream);
+    }
     switch (mode) {
         case kSample:
             return launch_pass_m<T, kSample, I>(var, tex_in, uv, kernel, klen, sh, lc, tex_out,
@@ -841,42 +992,6 @@ cudaError_t launch_pass_i(const Variant& var, int mode, const T* tex_in, const v
                                                     tex_out, codes, stream);
     }
     return cudaErrorInvalidValue;
-}
-
-template <typename T>
-cudaError_t launch_record_halves_t(const Variant& var, const void* uv, int klen, const Shape& sh,
-                                   const LaunchConfig& lc, uint32_t* codes,
-                                   cudaStream_t stream) {
-    if (!sh.small_index()) return cudaErrorInvalidValue;
-    const auto g = make_geometry<int32_t>(sh);
-    const auto tg = make_tiles<int32_t>(sh, lc, klen);
-    const auto cl = make_code_layout(sh, klen);
-    const int64_t count = lc.tile_count ? lc.tile_count : int64_t(tg.ntiles) - lc.tile_begin;
-    if (count <= 0) return cudaSuccess;
-    if (2 * count > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    const auto* p = static_cast<const typename Vec2<T>::type*>(uv);
-    const dim3 grid(unsigned(2 * count)), block(lc.block_x, lc.block_y);
-    const int code = (var.fma ? 4 : 0) | (var.branchless ? 2 : 0) | (var.pol ? 1 : 0);
-#define RLIC_HALVES_CASE(C, F, B, P)                                                         \
-    case C:                                                                                  \
-        lic_record_halves_kernel<T, F, B, P, int32_t><<<grid, block, 0, stream>>>(           \
-            p, klen, g, tg, codes, cl, lc.field_nan);                                        \
-        break;
-    switch (code) {
-        RLIC_HALVES_CASE(0, false, false, false)
-        RLIC_HALVES_CASE(1, false, false, true)
-        RLIC_HALVES_CASE(2, false, true, false)
-        RLIC_HALVES_CASE(3, false, true, true)
-        RLIC_HALVES_CASE(4, true, false, false)
-        RLIC_HALVES_CASE(5, true, false, true)
-        RLIC_HALVES_CASE(6, true, true, false)
-        RLIC_HALVES_CASE(7, true, true, true)
-        default:
-            return cudaErrorInvalidValue;
-    }
-#undef RLIC_HALVES_CASE
-    count_launch();
-    return cudaGetLastError();
 }
 
 template <typename T, bool FMA, typename I>
@@ -1075,12 +1190,6 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
                                                        tex_out, stream)                      \
                    : launch_gather_t<T, false, int64_t>(tex_in, codes, kernel, klen, sh, lc, \
                                                         tex_out, stream);                    \
-    }                                                                                        \
-    cudaError_t launch_record_halves(const Variant& var, const T* /*type tag*/,              \
-                                     const void* uv, int klen, const Shape& sh,              \
-                                     const LaunchConfig& lc, uint32_t* codes,                \
-                                     cudaStream_t stream) {                                  \
-        return launch_record_halves_t<T>(var, uv, klen, sh, lc, codes, stream);              \
     }                                                                                        \
     cudaError_t launch_trace_cells(const Variant& var, const T* /*type tag*/, const void* uv, \
                                    const Shape& sh, int klen, int64_t npix,                  \

@@ -36,6 +36,9 @@ struct LaunchConfig {
     // traced passes only: device flag that the pack kernels set when the
     // field holds a NaN sample (null: unknown, so every step checks)
     const unsigned* field_nan = nullptr;
+    // traced passes only: trace each pixel's two half-streamlines on two
+    // threads (lic_pass_paired_kernel), where the launch fits that form
+    bool paired = false;
 };
 
 // What a traced pass does per step: sample the texture, sample and record the
@@ -64,6 +67,27 @@ inline int64_t code_words_per_pixel(int64_t klen) {
     return (nf + 7) / 8 + (kmid + 7) / 8;
 }
 
+// Whether a traced pass over an image of npix pixels with CTAs of
+// block_x x block_y pixels and a kernel of klen taps fits the paired form
+// (lic_pass_paired_kernel: two threads per pixel, at most 128 threads per
+// CTA, the backward samples of a CTA's pixels within 96 KiB of shared
+// memory, 32-bit pixel indices, at least one tap per half).
+constexpr int kPairedMaxThreadsHost = 128;
+constexpr size_t kPairedSmemMax = 96 * 1024;
+inline size_t paired_smem_bytes(int64_t klen, int npx, size_t elem) {
+    const int64_t kmid = klen / 2;
+    const int64_t nf = klen - kmid - 1;
+    return elem * size_t(((nf + 7) & ~int64_t(7)) + ((kmid + 7) & ~int64_t(7))) +
+           elem * size_t(kmid) * size_t(npx);
+}
+inline bool paired_launch_fits(int64_t npix, int block_x, int block_y, int64_t klen,
+                               size_t elem) {
+    const int npx = block_x * block_y;
+    return npix < (int64_t(1) << 31) - 1 && klen >= 3 && klen <= (int64_t(1) << 20) &&
+           npx % 16 == 0 && 2 * npx <= kPairedMaxThreadsHost &&
+           paired_smem_bytes(klen, npx, elem) <= kPairedSmemMax;
+}
+
 #define RLIC_DECLARE_LAUNCHERS(T)                                                          \
     cudaError_t launch_pack(const T* u, const T* v, void* uv, int64_t n, cudaStream_t stream, \
                             unsigned* nan_flag = nullptr);                                 \
@@ -74,9 +98,6 @@ inline int64_t code_words_per_pixel(int64_t klen) {
     cudaError_t launch_gather(bool fma, const T* tex_in, const uint32_t* codes,            \
                               const T* kernel, int klen, const Shape& sh,                  \
                               const LaunchConfig& lc, T* tex_out, cudaStream_t stream);    \
-    cudaError_t launch_record_halves(const Variant& var, const T* type_tag, const void* uv, \
-                                     int klen, const Shape& sh, const LaunchConfig& lc,    \
-                                     uint32_t* codes, cudaStream_t stream);                \
     cudaError_t launch_trace_cells(const Variant& var, const T* type_tag, const void* uv,  \
                                    const Shape& sh, int klen, int64_t npix,                \
                                    const int64_t* pix, int64_t* cells, cudaStream_t stream); \

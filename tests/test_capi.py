@@ -132,6 +132,9 @@ def test_block_shape_validation(native) -> None:
     assert native.rlic_set_block_shape(0, 4) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 64) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_block_shape(64, 4) == _native.RLIC_OK
+    assert native.rlic_set_block_shape(0, 0) == _native.RLIC_OK  # back to the defaults
+    assert native.rlic_set_split_pixels(-2) == _native.RLIC_ERR_INVALID_ARGUMENT
+    assert native.rlic_set_split_pixels(-1) == _native.RLIC_OK  # the default threshold
     assert native.rlic_set_replay_mode(7, 0) == _native.RLIC_ERR_INVALID_ARGUMENT
     assert native.rlic_set_replay_mode(_native.RLIC_REPLAY_STAGED, 6) == \
         _native.RLIC_ERR_INVALID_ARGUMENT

@@ -148,46 +148,6 @@ def test_staged_on_the_benchmark_field(staged) -> None:
     assert _native.lib().rlic_stage_timeouts() == 0
 
 
-@pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("bnd", BOUNDS, ids=str)
-def test_split_halves_equal_the_traced_pass(oracle, dtype, bnd) -> None:
-    """Small images trace their first pass as split halves (one thread per
-    half-streamline, recording codes) and replay it: the same bits as one
-    traced pass and as the oracle, for one and for three passes, with NaN
-    stops in the field."""
-    tex, u, v = _field(150, 172, dtype, seed=17, nans=True)
-    k = np.hanning(31).astype(dtype)
-    try:
-        for iters in (1, 3):
-            _native.set_split_pixels(1 << 19)
-            split = _run(tex, u, v, k, bnd, iters, _native.RLIC_REPLAY_AUTO)
-            _native.set_split_pixels(0)
-            fused = _run(tex, u, v, k, bnd, iters, _native.RLIC_REPLAY_AUTO)
-            assert _same_bits(split, fused), iters
-            want = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries=bnd,
-                                   iterations=iters)
-            assert _same_bits(split, want), iters
-    finally:
-        _native.set_split_pixels(0)
-        _native.set_replay_mode(_native.RLIC_REPLAY_AUTO)
-
-
-def test_split_halves_through_host_arrays(oracle) -> None:
-    """The README case from numpy arrays (broadcast u, v read in place),
-    with the split first pass switched on: the host path splits too."""
-    from rlic_gb300.workloads import readme_case
-
-    c = readme_case()
-    try:
-        _native.set_split_pixels(1 << 19)
-        got = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
-                                  boundaries="periodic")
-    finally:
-        _native.set_split_pixels(0)
-    want = oracle.convolve(c["texture"], c["u"], c["v"], c["kernel"], boundaries="periodic")
-    assert _same_bits(got, want)
-
-
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("bnd", ["closed", {"x": "periodic", "y": "closed"}], ids=str)
