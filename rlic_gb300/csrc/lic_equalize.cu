@@ -547,8 +547,9 @@ __device__ __forceinline__ void sliding_hist_run(const T* __restrict__ x,
     if (j >= nx) return;  // (each thread works on its own words only)
     const int64_t i0 = int64_t(blockIdx.y) * rows;
     const int64_t i1 = i0 + rows < ny ? i0 + rows : ny;
-    const int64_t cl = j - tw / 2 < 0 ? 0 : j - tw / 2;
-    const int64_t cr = j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw;
+    // window columns [cl, cr) as 32-bit offsets (a row has fewer than 2^31)
+    const int cl = int(j - tw / 2 < 0 ? 0 : j - tw / 2);
+    const int cr = int(j - tw / 2 + tw > nx ? nx : j - tw / 2 + tw);
     int32_t nvalid = 0;
     // adds (SIGN 1) or removes (SIGN -1) one cell of bin b: word b / 2, half
     // b % 2.  A non-finite cell (b = -1, only when !ALL_FINITE) adds 0 to
@@ -575,7 +576,7 @@ __device__ __forceinline__ void sliding_hist_run(const T* __restrict__ x,
     // any is applied, so that 8 loads are in flight
     auto row_update = [&](int64_t r, int sign) {
         const int32_t* p = bins + r * nx;
-        int64_t c = cl;
+        int c = cl;
         for (; c + 8 <= cr; c += 8) {
             int32_t b[8];
 #pragma unroll
@@ -591,7 +592,7 @@ __device__ __forceinline__ void sliding_hist_run(const T* __restrict__ x,
         const int64_t r1 = i0 - th / 2 + th > ny ? ny : i0 - th / 2 + th;
         for (int64_t r = r0; r < r1; ++r) row_update(r, 1);
     }
-    const int64_t c_span = cr - cl;
+    const int64_t c_span = int64_t(cr - cl);
     for (int64_t i = i0; i < i1; ++i) {
         if (i > i0) {
             const int64_t r_out = i - 1 - th / 2, r_in = i - th / 2 + th - 1;
@@ -715,7 +716,7 @@ cudaError_t launch_equalize_t(const T* x, int64_t ny, int64_t nx, int nbins, int
         map_tiles_kernel<T><<<dim3(unsigned((nx + 255) / 256), unsigned(gy)), 256, 0, stream>>>(
             x, bins, ny, nx, ntx, nbins, a0, a1, f, maps, out);
         count_launch();
-    } else if (nbins <= 256 && th * tw <= 65535) {
+    } else if (nbins <= 256 && th * tw <= 65535 && nx < (int64_t(1) << 30)) {
         // running window histograms: one wave of CTAs, each sliding its
         // 128 columns down one run of rows (the first window of a run costs
         // th * tw cells, every later one 2 tw), runs of at least 32 rows
