@@ -641,6 +641,10 @@ def run_readme(args) -> None:
 
     steps = max(args.steps, 50)
     ms = _time_calls(call, steps, args.warmup, stream)
+    # the same calls with one thread per pixel (no paired pass), for comparison
+    _native.set_split_pixels(0)
+    ms_one_thread = _time_calls(call, steps, args.warmup, stream)
+    _native.set_split_pixels(-1)
     samples = n * n * klen
     for _ in range(max(3, args.warmup)):
         res = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
@@ -660,6 +664,7 @@ def run_readme(args) -> None:
     print(json.dumps({
         "metric": METRIC, "unit": UNIT, "workload": "readme_256x256_f64_triangle65_periodic_velocity_n1",
         "value": samples / (ms / 1e3) / 1e9, "ms_per_call": ms, "dtype": "f64", "steps": steps,
+        "forms": {"paired": {"ms_per_call": ms}, "one_thread_per_pixel": {"ms_per_call": ms_one_thread}},
         "e2e": {"value": samples / (e2e_ms / 1e3) / 1e9, "ms_per_call": e2e_ms},
         "cpu_oracle_gsamples": {f"{k}_threads": v for k, v in res.items()},
     }), flush=True)
