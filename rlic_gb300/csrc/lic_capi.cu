@@ -183,9 +183,9 @@ constexpr int64_t kPairedSmallTilePixels = int64_t(1) << 17;
 // the greatest priority: the block scheduler then gives the upload kernels
 // the SM slots that the traced pass's blocks free, instead of queueing them
 // behind the whole pass.
-cudaStream_t aux_stream(cudaError_t* err) {
+cudaStream_t aux_stream(cudaError_t* err, bool greatest_priority = true) {
     static std::mutex mu;
-    static cudaStream_t streams[64] = {};
+    static cudaStream_t streams[2][64] = {};
     int dev = 0;
     *err = cudaGetDevice(&dev);
     if (*err != cudaSuccess) return nullptr;
@@ -194,14 +194,16 @@ cudaStream_t aux_stream(cudaError_t* err) {
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(mu);
-    if (!streams[dev]) {
+    cudaStream_t& s = streams[greatest_priority ? 0 : 1][dev];
+    if (!s) {
         int least = 0, greatest = 0;
         *err = cudaDeviceGetStreamPriorityRange(&least, &greatest);
         if (*err != cudaSuccess) return nullptr;
-        *err = cudaStreamCreateWithPriority(&streams[dev], cudaStreamNonBlocking, greatest);
+        *err = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking,
+                                            greatest_priority ? greatest : least);
         if (*err != cudaSuccess) return nullptr;
     }
-    return streams[dev];
+    return s;
 }
 
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
@@ -518,7 +520,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
     // rows, wrapped across a periodic edge) have arrived, so the upload
     // overlaps the traced pass.
     std::vector<cudaEvent_t> events;
-    cudaStream_t aux = nullptr;
+    cudaStream_t aux = nullptr, second = nullptr;
     auto body = [&]() -> int {
         RLIC_CUDA_TRY(cudaMemcpyAsync(d_kernel, kernel, size_t(klen) * sizeof(T),
                                       cudaMemcpyHostToDevice, stream));
@@ -541,14 +543,20 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
             if (!(wraps_y && nchunks > 1 && c == nchunks - 1)) order.push_back(c);
         std::vector<int> arrival(nchunks, 0);
         for (int k = 0; k < nchunks; ++k) arrival[order[k]] = k;
-        events.resize(nchunks + 1, nullptr);
+        events.resize(nchunks + 2, nullptr);
         for (auto& ev : events) RLIC_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        // the traced pass's groups of tile rows alternate between `stream` and
+        // a second stream, so that one group's last CTAs overlap the next
+        // group's first ones (launches on one stream would each drain first)
+        second = nchunks > 1 ? aux_stream(&e, false) : nullptr;
+        if (nchunks > 1 && !second) return cuda_fail(e, "cudaStreamCreate");
         // the packs OR into the field's NaN flag; the traced pass reads it
         unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
         RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
         // the scratch was allocated stream-ordered on `stream`
         RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
         RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
+        if (second) RLIC_CUDA_TRY(cudaStreamWaitEvent(second, events[nchunks], 0));
         unsigned char* uvb = ws + wl.uv;
         const bool cache = use_path_cache(iterations, klen, flags);
         const Shape sh = make_shape(ny, nx, bnd);
@@ -606,7 +614,9 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 }
             }
             RLIC_CUDA_TRY(cudaEventRecord(events[k], aux));
-            // first pass over the tile rows this arrival completes, by runs
+            // first pass over the tile rows this arrival completes, by runs,
+            // on the stream of this arrival's turn
+            cudaStream_t ps = (second && (k & 1)) ? second : stream;
             bool waited = false;
             for (int64_t tr = 0; tr < tile_rows;) {
                 if (need[tr] != k) {
@@ -615,7 +625,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 }
                 int64_t tr_end = tr + 1;
                 while (tr_end < tile_rows && need[tr_end] == k) ++tr_end;
-                if (!waited) RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[k], 0));
+                if (!waited) RLIC_CUDA_TRY(cudaStreamWaitEvent(ps, events[k], 0));
                 waited = true;
                 LaunchConfig part = lc;
                 part.tile_begin = tr * tiles_x;
@@ -624,9 +634,13 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 // from these tile rows, so the flag's value now suffices
                 part.field_nan = nan_flag;
                 RLIC_CUDA_TRY(rlic::launch_pass(var, mode, d_tex, uvb, d_kernel, int(klen), sh,
-                                                part, dst_of(0), codes, stream));
+                                                part, dst_of(0), codes, ps));
                 tr = tr_end;
             }
+        }
+        if (second) {  // the second stream's launches end before the passes that follow
+            RLIC_CUDA_TRY(cudaEventRecord(events[nchunks + 1], second));
+            RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks + 1], 0));
         }
         RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks - 1], 0));
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
@@ -655,6 +669,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
     rc = body();
     // an upload still queued after a failure must end before the scratch is released
     if (rc != RLIC_OK && aux) cudaStreamSynchronize(aux);
+    if (rc != RLIC_OK && second) cudaStreamSynchronize(second);
     unsigned negative = 0;
     cudaError_t ec = cudaSuccess;
     if (rc == RLIC_OK && (flags & RLIC_FLAG_CHECK_TEXTURE))
