@@ -186,3 +186,32 @@ def test_paired_sweep_records_the_same_path_cache(restore_knobs) -> None:
         results.append((out, codes))
     assert torch.equal(results[0][1], results[1][1])
     assert torch.equal(results[0][0].view(torch.int64), results[1][0].view(torch.int64))
+
+
+def test_paired_with_chunked_host_upload(oracle, restore_knobs) -> None:
+    """A host call of 4 Mpx and more uploads in row chunks and launches the
+    traced pass per group of tile rows, alternating two streams; with 8 x 8
+    CTAs and the paired threshold raised, those launches take the paired
+    form.  Same bits as the device-resident one-thread pass and the oracle,
+    across a periodic y seam (the last chunk goes first)."""
+    import torch
+
+    rng = np.random.default_rng(21)
+    ny, nx = 2101, 2050
+    tex = rng.random((ny, nx), dtype=np.float32)
+    u = (rng.random((ny, nx)) - 0.5).astype(np.float32)
+    v = (rng.random((ny, nx)) - 0.5).astype(np.float32)
+    k = np.hanning(15).astype(np.float32)
+    bnd = {"x": "closed", "y": "periodic"}
+    kw = dict(uv_mode="polarization", boundaries=bnd, iterations=2)
+    _native.set_split_pixels(0)
+    want = rlic_gb300.convolve(torch.from_numpy(tex).cuda(), torch.from_numpy(u).cuda(),
+                               torch.from_numpy(v).cuda(), kernel=torch.from_numpy(k).cuda(),
+                               **kw).cpu().numpy()
+    _native.set_block_shape(8, 8)
+    _native.set_split_pixels(ALL)
+    got = rlic_gb300.convolve(tex, u, v, kernel=k, **kw)
+    assert _same_bits(got, want)
+    full = oracle.convolve(tex, u, v, k, uv_mode="polarization", boundaries=bnd, iterations=2,
+                           nthreads=oracle.env_threads())
+    assert _same_bits(got, full)
