@@ -502,6 +502,17 @@ RLIC_API int rlic_check_quotients_f64(const double *a, const double *b, int64_t 
                                       int32_t *certified, void *stream);
 
 /*
+ * Self-check of the float64 streamline step's integer numerator (no
+ * reference counterpart): for each f[i] sets in_range[i] to 1 when
+ * 0 <= f[i] <= 1 (sign bit clear), and then g[i] to the step's value of
+ * fma(2, 0.5 - f[i], f[i]) computed with integer instructions, which must
+ * equal the IEEE result; otherwise in_range[i] = 0 and g[i] = 0.  Device
+ * pointers; asynchronous on `stream`.
+ */
+RLIC_API int rlic_check_numerators_f64(const double *f, int64_t n, double *g,
+                                       int32_t *in_range, void *stream);
+
+/*
  * Number of this library's kernels launched since load (all threads).  Lets
  * a caller confirm that work ran on the device and count launches per call.
  */

@@ -99,6 +99,7 @@ SIGNATURES: dict[str, tuple[list, object]] = {
     "rlic_convolve_f32_noalloc": ([_P, _P, _P, _I64, _I64, _P, _I64, _INT, _INT, _INT, _INT,
                                    _INT, _I64, _P, _P, _U], _INT),
     "rlic_check_quotients_f64": ([_P, _P, _I64, _P, _P, _P], _INT),
+    "rlic_check_numerators_f64": ([_P, _I64, _P, _P, _P], _INT),
     "rlic_equalize_histogram_f32": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_equalize_histogram_f64": ([_P, _I64, _I64, _I64, _INT, _I64, _I64, _P, _P, _U], _INT),
     "rlic_set_block_shape": ([_INT, _INT], _INT),

@@ -1597,6 +1597,17 @@ int rlic_check_quotients_f64(const double* a, const double* b, int64_t n, double
     return RLIC_OK;
 }
 
+int rlic_check_numerators_f64(const double* f, int64_t n, double* g, int32_t* in_range,
+                              void* stream) {
+    g_last_error.clear();
+    if (n < 0) return fail(RLIC_ERR_INVALID_ARGUMENT, "n must be >= 0");
+    if (n > 0 && (!f || !g || !in_range))
+        return fail(RLIC_ERR_INVALID_ARGUMENT, "null array pointer");
+    RLIC_CUDA_TRY(rlic::launch_numerator_check(f, n, g, in_range,
+                                               static_cast<cudaStream_t>(stream)));
+    return RLIC_OK;
+}
+
 uint64_t rlic_kernel_launch_count(void) { return rlic::launches(); }
 
 void* rlic_host_buffer_alloc(size_t bytes) {

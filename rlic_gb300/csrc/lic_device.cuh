@@ -286,14 +286,84 @@ __device__ __forceinline__ double known_numerator(double vel, double frac, bool 
     return centre ? 0.5 : ((s2 != one) ? 1.0 : 0.0);
 }
 
-// Both numerators of a float64 step, computing in FP64 only the one of the
-// axis whose fraction is not known exactly (the axis not moved last; x
-// before the first move, when both are 0.5).
-template <bool FMA>
+// The numerator fma(2, 0.5 - f, f) (1 + signum(v) = 2: the sign bit of v
+// clear) rounded to nearest, for 0 <= f <= 1, with integer instructions
+// only.  The FP64 pipe bounds the float64 step, and this replaces its
+// subtraction and its FMA.  Returns false, leaving g unset, for f outside
+// [0, 1] (the sign bit set, -0 included), where the caller uses FP64.
+//
+// With f = m 2^(E - 1075) (E its biased exponent, m its 53-bit
+// significand), d = RN(0.5 - f) and g = RN(2 d + f):
+//   * f = 1: 2 (0.5 - 1) + 1 = +0;
+//   * f in [0.5, 1): d = 0.5 - f exactly (Sterbenz), so g = 1 - f exactly,
+//     r 2^-53 with r = 2^53 - m, normalised by its leading zeros;
+//   * f in [2^-55, 0.5): d lies in [0.25, 0.5], a multiple of 2^-54.  With
+//     s1 = 1021 - E, f = (K + lo1 / 2^s1) 2^-54 for K = m >> s1, and
+//     d = (2^53 - K - c1) 2^-54, c1 rounding the remainder lo1 against
+//     half a unit h1 = 2^(s1-1) (ties to the even D; s1 = 0, f in
+//     [0.25, 0.5), is exact).  In units of 2^-53, 2 d + f = 2^53 - K - c1 +
+//     K / 2 exactly plus the remainder (K odd: half a unit and lo1), so
+//     g = (2^53 - ceil(K / 2) - c1 + c2) 2^-53, c2 rounding that remainder
+//     (ties to even); a result of 2^53 units is 1.0;
+//   * f < 2^-55 (subnormals and zero included): d = 0.5 and g = RN(1 + f)
+//     = 1.
+// Checked against the FP64 sequence on random and constructed operands,
+// rounding ties included (rlic_check_numerators_f64).
+constexpr uint64_t kMant52 = (uint64_t(1) << 52) - 1;
+constexpr uint64_t kOneBits64 = 0x3FF0000000000000ull;
+
+__device__ __forceinline__ bool numerator_two_int(double f, double& g) {
+    const uint64_t b = bits_of(f);
+    const uint32_t E = uint32_t(b >> 52);  // the sign bit included: f < 0 gives E >= 2048
+    const uint64_t m = (b & kMant52) | (uint64_t(1) << 52);
+    // f in [0.5, 1)
+    const uint64_t r1 = (uint64_t(1) << 53) - m;
+    const int lz = __clzll(r1 | 1u);
+    const uint64_t g_half = (uint64_t(uint32_t(1033 - lz) & 0x7FFu) << 52) |
+                            ((r1 << (lz > 11 ? lz - 11 : 0)) & kMant52);
+    // f in [2^-55, 0.5)
+    int s1 = 1021 - int(E);
+    s1 = s1 < 0 ? 0 : (s1 > 53 ? 53 : s1);
+    const uint64_t K = m >> s1;
+    const uint64_t lo1 = m & ((uint64_t(1) << s1) - 1);
+    const uint64_t h1 = (uint64_t(1) << s1) >> 1;
+    const uint64_t c1 = (s1 > 0 && (lo1 > h1 || (lo1 == h1 && (K & 1)))) ? 1u : 0u;
+    const uint64_t G0 = (uint64_t(1) << 53) - ((K + 1) >> 1) - c1;
+    const uint64_t c2 = ((K & 1) && (lo1 != 0 || (G0 & 1))) ? 1u : 0u;
+    const uint64_t G = G0 + c2;
+    const uint64_t g_low =
+        G >= (uint64_t(1) << 53) ? kOneBits64 : ((uint64_t(1022) << 52) | (G & kMant52));
+    uint64_t r = E < 968u ? kOneBits64 : (E <= 1021u ? g_low : g_half);
+    r = b == kOneBits64 ? 0u : r;
+    g = from_bits(r);
+    return E < 1023u || b == kOneBits64;
+}
+
+// Both numerators of a float64 step, computing only the one of the axis
+// whose fraction is not known exactly (the axis not moved last; x before
+// the first move, when both are 0.5): f when the velocity's sign bit is set
+// (1 + signum(v) = 0: 0 (0.5 - f) + f = f), otherwise by integer
+// instructions (numerator_two_int), and with FP64 instructions only for a
+// fraction outside [0, 1].  The branchless build without `fma` rounds
+// 2 (0.5 - f) exactly and then the sum, the same value.
+// INT_NUM = false computes it with FP64 instructions instead (the paired
+// pass on small images, which waits on latency more than on the FP64 pipe:
+// the integer sequence lengthens each step's chain there).
+template <bool FMA, bool INT_NUM = true>
 __device__ __forceinline__ void time_numerators(double u, double v, double fx, double fy,
                                                 int last, double& ax, double& ay) {
     const bool gen_y = (last == kLastX);
-    const double g = time_numerator<double, FMA>(gen_y ? v : u, gen_y ? fy : fx);
+    const double vel = gen_y ? v : u;
+    const double frac = gen_y ? fy : fx;
+    double g;
+    if constexpr (INT_NUM) {
+        g = frac;
+        if (!sign_set(vel)) {
+            if (!numerator_two_int(frac, g)) g = time_numerator<double, FMA>(vel, frac);
+        }
+    } else {
+        g = time_numerator<double, FMA>(vel, frac);
+    }
     const double k = known_numerator(gen_y ? u : v, gen_y ? fx : fy, last == kLastNone);
     ax = gen_y ? k : g;
     ay = gen_y ? g : k;
@@ -527,7 +597,7 @@ __device__ __forceinline__ void fill_delta_table(I* table, I nx, I ny) {
 // range already, and the rule is the identity on in-range coordinates).
 //
 // Returns the step code (see above).
-template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I>
+template <typename T, bool FMA, bool BRANCHLESS, bool EDGE, typename I, bool INT_NUM = true>
 __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& i, I& j,
                                             int& last, const Geometry<I>& g) {
     const bool still = is_zero(u) & is_zero(v);
@@ -545,7 +615,7 @@ __device__ __forceinline__ uint32_t advance(T u, T v, T& fx, T& fy, I& cell, I& 
         // one division when the screen settles the comparison, else both;
         // one numerator computed in FP64 (see known_numerator)
         T ax, ay;
-        time_numerators<FMA>(su, sv, fx, fy, last, ax, ay);
+        time_numerators<FMA, INT_NUM>(su, sv, fx, fy, last, ax, ay);
         const bool settled = screen_step(ax, ay, su, sv, xstep);
         const bool first_x = !settled || xstep;
         const T num = first_x ? ax : ay;
@@ -689,8 +759,9 @@ __device__ __forceinline__ double neg_if(double x, bool n) {
 // rounded products and a rounded sum, src/lib.rs:341), negate it for the
 // backward trace, advance, then accumulate weight * texture at the new cell.
 // `code` receives the step code; `x_out`, when given, the texture sample.
+// INT_NUM: see time_numerators (float64 only).
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, int DIR, bool EDGE,
-          bool SAMPLE, typename I, bool NAN_CHECK = true, bool NC = true>
+          bool SAMPLE, typename I, bool NAN_CHECK = true, bool NC = true, bool INT_NUM = true>
 __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
                                            const Geometry<I>& g,
                                            const typename Vec2<T>::type* __restrict__ uv,
@@ -722,8 +793,8 @@ __device__ __forceinline__ bool trace_step(TraceState<T, I>& st, T& acc, T w,
         pu = neg_if(pu, st.back);
         pv = neg_if(pv, st.back);
     }
-    code = advance<T, FMA, BRANCHLESS, EDGE>(pu, pv, st.fx, st.fy, st.cell, st.i, st.j, st.last,
-                                             g);
+    code = advance<T, FMA, BRANCHLESS, EDGE, I, INT_NUM>(pu, pv, st.fx, st.fy, st.cell, st.i,
+                                                         st.j, st.last, g);
     if constexpr (SAMPLE) {
         const T x = ld_in<NC>(tex + st.cell);
         acc = accumulate<T, FMA>(w, x, acc);

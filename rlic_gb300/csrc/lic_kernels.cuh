@@ -255,7 +255,8 @@ __device__ __forceinline__ int trace_paired_half(T& acc, I i, I j, bool back,
             if (b < n) {
                 uint32_t code = 0;
                 T x;
-                if (!trace_step<T, FMA, BRANCHLESS, POL, kDirRuntime, EDGE, true, I, NAN_CHECK>(
+                if (!trace_step<T, FMA, BRANCHLESS, POL, kDirRuntime, EDGE, true, I, NAN_CHECK,
+                                true, false>(
                         st, acc, wq[b], g, uv, tex, code, &x)) {
                     if constexpr (RECORD) words[size_t(q) * stride] = word | (kStop << (4 * b));
                     return 8 * q + b;

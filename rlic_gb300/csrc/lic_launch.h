@@ -161,6 +161,9 @@ cudaError_t stage_timeout_seen(bool* seen);
 // Self-check of the screened float64 division (lic_kernels_f64.cu).
 cudaError_t launch_quotient_check(const double* a, const double* b, int64_t n, double* q,
                                   int32_t* certified, cudaStream_t stream);
+// Self-check of the float64 step's integer numerator (lic_kernels_f64.cu).
+cudaError_t launch_numerator_check(const double* f, int64_t n, double* g, int32_t* in_range,
+                                   cudaStream_t stream);
 
 #undef RLIC_DECLARE_LAUNCHERS
 
