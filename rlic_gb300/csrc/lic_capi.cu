@@ -158,8 +158,14 @@ cudaMemPool_t library_pool(cudaError_t* err) {
     return pools[dev];
 }
 
+// Upload chunks of a host-memory call: at most this many, each of at least
+// max(K - 1, 64) rows and 2^20 pixels.  Measured end to end at 8192^2
+// float32, 65 taps, 5 passes (ms per call, traced-pass groups alternating
+// two streams): 6 chunks 17.23, 8 17.08, 12 16.92, 16 16.85, 20 16.81,
+// 24 16.79, 32 16.76 (the first traced rows start after a smaller first
+// chunk).
 #ifndef RLIC_HOST_CHUNKS
-#define RLIC_HOST_CHUNKS 8
+#define RLIC_HOST_CHUNKS 32
 #endif
 
 // Images of at most this many pixels trace their passes with each pixel's
@@ -528,13 +534,14 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         aux = aux_stream(&e);
         if (!aux) return cuda_fail(e, "cudaStreamCreate");
         const int64_t R = klen / 2;
-        // up to RLIC_HOST_CHUNKS chunks of at least max(2R, 64) rows, for
-        // images of 4 Mpx and more
+        // up to RLIC_HOST_CHUNKS chunks of at least max(2R, 64) rows and
+        // 2^20 pixels, for images of 4 Mpx and more
         const int nchunks =
             n < (size_t(1) << 22)
                 ? 1
-                : int(std::min<int64_t>(RLIC_HOST_CHUNKS,
-                                        std::max<int64_t>(1, ny / std::max<int64_t>(2 * R, 64))));
+                : int(std::max<int64_t>(
+                      1, std::min<int64_t>(std::min<int64_t>(RLIC_HOST_CHUNKS, int64_t(n >> 20)),
+                                           ny / std::max<int64_t>(2 * R, 64))));
         const int64_t rows_per = (ny + nchunks - 1) / nchunks;
         const bool wraps_y = bnd[2] == RLIC_BOUNDARY_PERIODIC || bnd[3] == RLIC_BOUNDARY_PERIODIC;
         std::vector<int> order;
