@@ -171,9 +171,9 @@ cudaMemPool_t library_pool(cudaError_t* err) {
 // Images of at most this many pixels trace their passes with each pixel's
 // two half-streamlines on two threads (lic_pass_paired_kernel) unless
 // rlic_set_split_pixels chose a threshold.  Measured on GB300, calls of one
-// pass on device memory (ms): float64 256^2, 65 taps 0.103 (4 x 4-pixel
-// tiles) against 0.114-0.117 with one thread per pixel, 512^2 0.347 against
-// 0.374; float32 256^2 0.028 against 0.030, 512^2 0.064 against 0.058.  The
+// pass on device memory (ms): float64 256^2, 65 taps 0.0957 (4 x 4-pixel
+// tiles) against 0.114-0.117 with one thread per pixel, 512^2 0.336 against
+// 0.375; float32 256^2 0.028 against 0.030, 512^2 0.064 against 0.058.  The
 // paired form spends about 12% more FP64 instructions (the forward thread
 // adds the backward samples after its own), and the float32 pass is bound
 // by instruction issue, so it pays only where the image alone cannot fill

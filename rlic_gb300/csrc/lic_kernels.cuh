@@ -209,12 +209,6 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
     if constexpr (MODE != kRecordOnly) tex_out[i * g.nx + j] = acc;
 }
 
-// One half of a pixel's streamline for the paired pass below: the direction
-// is the thread's (st.back); every step's texture sample is accumulated into
-// `acc` with this half's weights `w` and, on backward threads, also stored
-// at sink[s * sink_stride] for step s.  Records step codes like trace_half.
-// Returns the number of steps sampled (count, or the step that met a NaN
-// sample and stopped the trace).
 // Steps of a code word unrolled in the paired pass's loop (8: the whole
 // word).  The float64 pass's unrolled steps overflow the instruction cache
 // (ncu: warps waiting on instruction fetch); 4 measured 7% faster than 8 on
@@ -228,6 +222,12 @@ lic_pass_kernel(const T* __restrict__ tex_in, const typename Vec2<T>::type* __re
 template <typename T> struct PairedUnroll { static constexpr int value = RLIC_PAIRED_UNROLL_F32; };
 template <> struct PairedUnroll<double> { static constexpr int value = RLIC_PAIRED_UNROLL_F64; };
 
+// One half of a pixel's streamline for the paired pass below: the direction
+// is the thread's (st.back); every step's texture sample is accumulated into
+// `acc` with this half's weights `w` and, on backward threads, also stored
+// at sink[s * sink_stride] for step s.  Records step codes like trace_half.
+// Returns the number of steps sampled (count, or the step that met a NaN
+// sample and stopped the trace).
 template <typename T, bool FMA, bool BRANCHLESS, bool POL, bool EDGE, bool RECORD, typename I,
           bool NAN_CHECK>
 __device__ __forceinline__ int trace_paired_half(T& acc, I i, I j, bool back,
