@@ -7,6 +7,12 @@ gradient back along the same recorded streamlines (d loss / d texture), and
 a per-tap reduction gives d loss / d kernel.  u and v are not
 differentiable: the streamline cells are discrete choices.
 
+``ConvolvePlan``: one ``convolve`` call on CUDA tensors recorded into a
+CUDA graph: the field's packing and every pass (the traced first pass, the
+replayed passes ping-ponging between the output and a workspace buffer) in
+one graph launch, for callers that convolve new textures over a fixed
+field and configuration repeatedly.
+
 ``convolve_lowp``: the reduced-precision form.  Streamline cells are traced
 in the input dtype (float64 inputs keep a float64 advance), then the texture
 and every buffer between passes are stored as FP16 or BF16 and each pass
@@ -20,7 +26,7 @@ and validate their inputs with the same rules and messages.
 
 from __future__ import annotations
 
-__all__ = ["convolve_autograd", "convolve_lowp"]
+__all__ = ["ConvolvePlan", "convolve_autograd", "convolve_lowp"]
 
 import ctypes
 from typing import Any
@@ -216,3 +222,88 @@ def convolve_autograd(
             texture.contiguous(), kernel.to(device=dev).contiguous(), u_c, v_c,
             _native.UV_MODE_CODES[uv_mode], bs.codes(), iterations,
         )
+
+
+# ------------------------------------------------------------- graph plan --
+
+class ConvolvePlan:
+    """``convolve`` on torch CUDA tensors, recorded into one CUDA graph.
+
+    The plan validates its arguments once, with ``convolve``'s rules and
+    messages, and owns device buffers for the texture, u, v, the kernel,
+    the output and the call's workspace.  ``run()`` launches the call on
+    the current stream (``rlic_convolve_f32/_f64`` on device memory: the
+    field's packing, the traced first pass, then the replayed passes,
+    alternating between the output and a workspace buffer); ``capture()``
+    records that call into a CUDA graph, and ``replay()`` re-runs it with
+    one graph launch and returns the output tensor (the same tensor every
+    time).  Between replays, write new values into ``plan.texture`` (or
+    ``plan.u``, ``plan.v``) in place; shapes, dtype, kernel length, uv mode,
+    boundaries and iterations are fixed.  New texture values are not
+    checked for negative entries (the validation ran once).  The result is
+    bit-identical to ``convolve`` on the same values.
+    """
+
+    def __init__(self, texture: Any, u: Any, v: Any, *, kernel: Any,
+                 uv_mode: str = "velocity", boundaries: Any = "closed", iterations: int = 1):
+        import torch
+
+        use_torch, bs = _validated(texture, u, v, kernel, uv_mode, boundaries, iterations)
+        if not use_torch:
+            raise TypeError("ConvolvePlan takes torch CUDA tensors")
+        dev = texture.device
+        if dev.type != "cuda":
+            raise ValueError("ConvolvePlan takes CUDA tensors")
+        self.device = dev
+        self.texture, self.u, self.v, self.kernel = (
+            a.detach().to(device=dev).contiguous().clone() for a in (texture, u, v, kernel))
+        self.iterations = int(iterations)
+        self.out = torch.empty_like(self.texture)
+        self.lib = _native.lib()
+        f32 = self.texture.dtype == torch.float32
+        self._fn = self.lib.rlic_convolve_f32 if f32 else self.lib.rlic_convolve_f64
+        ny, nx = self.texture.shape
+        klen = self.kernel.shape[0]
+        nbytes = self.lib.rlic_workspace_bytes(ny, nx, klen, max(self.iterations, 1),
+                                               4 if f32 else 8, 0)
+        self.workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+        self._args = (ny, nx, klen, _native.UV_MODE_CODES[uv_mode], bs.codes(), nbytes)
+        self.graph = None
+
+    def run(self) -> Any:
+        """Launch the call on the current stream; returns the output tensor."""
+        import torch
+
+        ny, nx, klen, uv_code, bcodes, nbytes = self._args
+        if self.iterations == 0:  # the texture itself, as convolve returns a copy
+            self.out.copy_(self.texture)
+            return self.out
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        _native.check(self._fn(
+            self.texture.data_ptr(), self.u.data_ptr(), self.v.data_ptr(), ny, nx,
+            self.kernel.data_ptr(), klen, uv_code, *bcodes, self.iterations, self.out.data_ptr(),
+            self.workspace.data_ptr(), nbytes, stream, 0))
+        return self.out
+
+    def capture(self) -> None:
+        """Record the call into a CUDA graph (replay() re-runs it).  One run
+        on the current stream first sets up everything a first call does."""
+        import torch
+
+        with torch.cuda.device(self.device):
+            self.run()
+            torch.cuda.synchronize(self.device)
+            side = torch.cuda.Stream(self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side), torch.cuda.graph(graph, stream=side):
+                self.run()
+            torch.cuda.current_stream(self.device).wait_stream(side)
+        self.graph = graph
+
+    def replay(self) -> Any:
+        """Re-run the recorded call; returns the output tensor."""
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        self.graph.replay()
+        return self.out
