@@ -645,6 +645,12 @@ def run_readme(args) -> None:
     _native.set_split_pixels(0)
     ms_one_thread = _time_calls(call, steps, args.warmup, stream)
     _native.set_split_pixels(-1)
+    # the call recorded into a CUDA graph (rlic_gb300.forms.ConvolvePlan)
+    from rlic_gb300.forms import ConvolvePlan
+
+    plan = ConvolvePlan(t["texture"], t["u"], t["v"], kernel=t["kernel"], boundaries="periodic")
+    plan.capture()
+    ms_graph = _time_calls(plan.replay, steps, args.warmup, stream)
     samples = n * n * klen
     for _ in range(max(3, args.warmup)):
         res = rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"],
@@ -664,7 +670,8 @@ def run_readme(args) -> None:
     print(json.dumps({
         "metric": METRIC, "unit": UNIT, "workload": "readme_256x256_f64_triangle65_periodic_velocity_n1",
         "value": samples / (ms / 1e3) / 1e9, "ms_per_call": ms, "dtype": "f64", "steps": steps,
-        "forms": {"paired": {"ms_per_call": ms}, "one_thread_per_pixel": {"ms_per_call": ms_one_thread}},
+        "forms": {"paired": {"ms_per_call": ms}, "one_thread_per_pixel": {"ms_per_call": ms_one_thread},
+                  "graph_replay": {"ms_per_call": ms_graph}},
         "e2e": {"value": samples / (e2e_ms / 1e3) / 1e9, "ms_per_call": e2e_ms},
         "cpu_oracle_gsamples": {f"{k}_threads": v for k, v in res.items()},
     }), flush=True)
