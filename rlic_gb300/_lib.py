@@ -66,6 +66,21 @@ class _Ops:
             return bool((~self._t.isfinite(a)).any())
         return bool(np.any(~np.isfinite(a)))
 
+    def scans(self, texture: Any, kernel: Any, check_negative: bool) -> tuple[bool, bool]:
+        """(any texture element < 0, any kernel element non-finite).  For
+        tensors on one device both reductions come back to the host in one
+        transfer (one synchronisation instead of two)."""
+        if not self.torch:
+            neg = self.any_negative(texture) if check_negative else False
+            return neg, self.any_nonfinite(kernel)
+        parts = [(texture < 0).any()] if check_negative else []
+        parts.append((~self._t.isfinite(kernel)).any())
+        if len({p.device for p in parts}) == 1:
+            vals = [bool(x) for x in self._t.stack(parts).tolist()]
+        else:
+            vals = [bool(p) for p in parts]
+        return (vals[0] if check_negative else False), vals[-1]
+
 
 _NEGATIVE_TEXTURE = "Found invalid texture element(s). Expected only positive values."
 
@@ -117,7 +132,8 @@ def _collect_problems(
         problems.append(
             ValueError(f"Expected a texture with exactly two dimensions. Got texture.ndim={texture.ndim!r}")
         )
-    if check_negative and ops.any_negative(texture):
+    negative, nonfinite_kernel = ops.scans(texture, kernel, check_negative)
+    if negative:
         problems.append(ValueError(_NEGATIVE_TEXTURE))
     tshape, ushape, vshape = ops.shape(texture), ops.shape(u), ops.shape(v)
     if ushape != tshape or vshape != tshape:
@@ -131,7 +147,7 @@ def _collect_problems(
         problems.append(
             ValueError(f"Expected a kernel with exactly one dimension. Got kernel.ndim={kernel.ndim!r}")
         )
-    if ops.any_nonfinite(kernel):
+    if nonfinite_kernel:
         problems.append(ValueError("Found non-finite value(s) in kernel."))
 
     bs = BoundarySet.from_spec(boundaries)
