@@ -531,8 +531,6 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         RLIC_CUDA_TRY(cudaMemcpyAsync(d_kernel, kernel, size_t(klen) * sizeof(T),
                                       cudaMemcpyHostToDevice, stream));
         cudaError_t e = cudaSuccess;
-        aux = aux_stream(&e);
-        if (!aux) return cuda_fail(e, "cudaStreamCreate");
         const int64_t R = klen / 2;
         // up to RLIC_HOST_CHUNKS chunks of at least max(2R, 64) rows and
         // 2^20 pixels, for images of 4 Mpx and more
@@ -550,20 +548,30 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
             if (!(wraps_y && nchunks > 1 && c == nchunks - 1)) order.push_back(c);
         std::vector<int> arrival(nchunks, 0);
         for (int k = 0; k < nchunks; ++k) arrival[order[k]] = k;
-        events.resize(nchunks + 2, nullptr);
-        for (auto& ev : events) RLIC_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        // one chunk (images under 4 Mpx): the upload and the passes run in
+        // order on `stream`, with no second stream and no events
+        const bool chunked = nchunks > 1;
+        aux = chunked ? aux_stream(&e) : stream;
+        if (!aux) return cuda_fail(e, "cudaStreamCreate");
+        if (chunked) {
+            events.resize(nchunks + 2, nullptr);
+            for (auto& ev : events)
+                RLIC_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        }
         // the traced pass's groups of tile rows alternate between `stream` and
         // a second stream, so that one group's last CTAs overlap the next
         // group's first ones (launches on one stream would each drain first)
-        second = nchunks > 1 ? aux_stream(&e, false) : nullptr;
-        if (nchunks > 1 && !second) return cuda_fail(e, "cudaStreamCreate");
+        second = chunked ? aux_stream(&e, false) : nullptr;
+        if (chunked && !second) return cuda_fail(e, "cudaStreamCreate");
         // the packs OR into the field's NaN flag; the traced pass reads it
         unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
         RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
         // the scratch was allocated stream-ordered on `stream`
-        RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
-        RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
-        if (second) RLIC_CUDA_TRY(cudaStreamWaitEvent(second, events[nchunks], 0));
+        if (chunked) {
+            RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
+            RLIC_CUDA_TRY(cudaStreamWaitEvent(aux, events[nchunks], 0));
+            RLIC_CUDA_TRY(cudaStreamWaitEvent(second, events[nchunks], 0));
+        }
         unsigned char* uvb = ws + wl.uv;
         const bool cache = use_path_cache(iterations, klen, flags);
         const Shape sh = make_shape(ny, nx, bnd);
@@ -620,7 +628,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                                                     aux, nan_flag));
                 }
             }
-            RLIC_CUDA_TRY(cudaEventRecord(events[k], aux));
+            if (chunked) RLIC_CUDA_TRY(cudaEventRecord(events[k], aux));
             // first pass over the tile rows this arrival completes, by runs,
             // on the stream of this arrival's turn
             cudaStream_t ps = (second && (k & 1)) ? second : stream;
@@ -632,7 +640,7 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 }
                 int64_t tr_end = tr + 1;
                 while (tr_end < tile_rows && need[tr_end] == k) ++tr_end;
-                if (!waited) RLIC_CUDA_TRY(cudaStreamWaitEvent(ps, events[k], 0));
+                if (!waited && chunked) RLIC_CUDA_TRY(cudaStreamWaitEvent(ps, events[k], 0));
                 waited = true;
                 LaunchConfig part = lc;
                 part.tile_begin = tr * tiles_x;
@@ -645,11 +653,11 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 tr = tr_end;
             }
         }
-        if (second) {  // the second stream's launches end before the passes that follow
+        if (chunked) {  // the second stream's launches and the last upload end first
             RLIC_CUDA_TRY(cudaEventRecord(events[nchunks + 1], second));
             RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks + 1], 0));
+            RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks - 1], 0));
         }
-        RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks - 1], 0));
         if (flags & RLIC_FLAG_CHECK_TEXTURE)
             RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
         const T* src = dst_of(0);
