@@ -244,10 +244,11 @@ LaunchConfig launch_config() { return LaunchConfig{g_block_x.load(), g_block_y.l
 // CTA shape of the traced passes.  Unless rlic_set_block_shape chose one,
 // traced passes use squarer tiles than the replay's 64 x 4: 16 x 8 pixels,
 // and 8 x 8 for images of at most kSmallImagePixels pixels, whose tiles are
-// too few to spread evenly over the SMs otherwise.  Measured (ms per pass):
-// 8192^2 float32 with recording 9.78 against 10.18 for 64 x 4; 1024^2
-// float64 1.20 against 1.34; 256^2 float64 0.117 against 0.161; 512^2
-// float32 0.059 against 0.062.
+// too few to spread evenly over the SMs otherwise (4 x 4 for the paired
+// pass on the smallest images, see kPairedSmallTilePixels).  Measured with
+// one thread per pixel (ms per pass): 8192^2 float32 with recording 9.78
+// against 10.18 for 64 x 4; 1024^2 float64 1.20 against 1.34; 256^2
+// float64 0.117 against 0.161; 512^2 float32 0.059 against 0.062.
 std::atomic<bool> g_block_custom{false};
 constexpr int64_t kSmallImagePixels = int64_t(1) << 19;
 
