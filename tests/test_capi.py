@@ -50,6 +50,11 @@ def test_workspace_bytes(native) -> None:
     assert ws(10, 10, 3, 2, 8, 0x8) == 1792 + 1024 + 256 + 256
     assert ws(0, 10, 3, 1, 4, 0) == 0
     assert ws(10, 10, 3, 1, 2, 0) == 0
+    # a small image traced by the paired pass keeps no path cache for one
+    # pass, whatever the paired threshold
+    for split in (1 << 40, 0, -1):
+        assert native.rlic_set_split_pixels(split) == 0
+        assert ws(256, 256, 65, 1, 8, 0) == 2 * 65536 * 8 + 768 + 256
 
 
 def test_path_code_bytes(native) -> None:
