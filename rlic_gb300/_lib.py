@@ -114,19 +114,21 @@ def _collect_problems(
             ValueError(f"Invalid uv_mode {uv_mode!r}. Expected one of {_KNOWN_UV_MODES}")
         )
 
-    expectation = (
-        "Expected texture, u, v and kernel with identical dtype, from "
-        f"{ops.supported}. Got texture.dtype={texture.dtype!r}, u.dtype={u.dtype!r}, "
-        f"v.dtype={v.dtype!r}, kernel.dtype={kernel.dtype!r}"
-    )
+    def expectation() -> str:  # built only when a dtype problem is reported
+        return (
+            "Expected texture, u, v and kernel with identical dtype, from "
+            f"{ops.supported}. Got texture.dtype={texture.dtype!r}, u.dtype={u.dtype!r}, "
+            f"v.dtype={v.dtype!r}, kernel.dtype={kernel.dtype!r}"
+        )
+
     dtypes = {a.dtype for a in (texture, u, v, kernel)}
     unsupported = dtypes.difference(ops.supported)
     if unsupported:
         problems.append(
-            TypeError(f"Found unsupported data type(s): {list(unsupported)}. {expectation}")
+            TypeError(f"Found unsupported data type(s): {list(unsupported)}. {expectation()}")
         )
     if len(dtypes) != 1:
-        problems.append(TypeError(f"Data types mismatch. {expectation}"))
+        problems.append(TypeError(f"Data types mismatch. {expectation()}"))
 
     if texture.ndim != 2:
         problems.append(
