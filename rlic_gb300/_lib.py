@@ -59,12 +59,12 @@ class _Ops:
     def any_negative(self, a: Any) -> bool:
         if self.torch:
             return bool((a < 0).any())
-        return bool(np.any(a < 0))
+        return bool((a < 0).any())
 
     def any_nonfinite(self, a: Any) -> bool:
         if self.torch:
             return bool((~self._t.isfinite(a)).any())
-        return bool(np.any(~np.isfinite(a)))
+        return not np.isfinite(a).all()
 
     def scans(self, texture: Any, kernel: Any, check_negative: bool) -> tuple[bool, bool]:
         """(any texture element < 0, any kernel element non-finite).  For
@@ -208,9 +208,12 @@ def _convolve_numpy(
         flags |= _native.RLIC_FLAG_CHECK_TEXTURE
     f32 = dtype == np.dtype("float32")
     views = (texture, u, v)
-    strides = [_element_strides(a) for a in views]
-    contiguous = all(a.flags.c_contiguous for a in views)
-    if not contiguous and all(s is not None for s in strides) and lib.rlic_host_direct_access():
+    strides = None
+    if not all(a.flags.c_contiguous for a in views):
+        strides = [_element_strides(a) for a in views]
+        if any(s is None for s in strides) or not lib.rlic_host_direct_access():
+            strides = None
+    if strides is not None:
         # strided views (broadcasts, transposes, slices) are read in place
         st = (ctypes.c_int64 * 6)(*(x for s in strides for x in s))
         fn = lib.rlic_convolve_strided_f32 if f32 else lib.rlic_convolve_strided_f64

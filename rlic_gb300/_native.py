@@ -9,6 +9,7 @@ missing or cannot be loaded, every call that needs it raises
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import threading
 import weakref
@@ -184,7 +185,8 @@ def pinned_empty(shape: tuple, dtype) -> "np.ndarray":
     import numpy as np
 
     dtype = np.dtype(dtype)
-    nbytes = int(np.prod(shape)) * dtype.itemsize
+    count = math.prod(shape)
+    nbytes = count * dtype.itemsize
     L = lib()
     ptr = L.rlic_host_buffer_alloc(max(nbytes, 1))
     if not ptr:
@@ -192,7 +194,7 @@ def pinned_empty(shape: tuple, dtype) -> "np.ndarray":
     buf = (ctypes.c_char * max(nbytes, 1)).from_address(ptr)
     free = L.rlic_host_buffer_free
     weakref.finalize(buf, free, ctypes.c_void_p(ptr))
-    arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+    arr = np.frombuffer(buf, dtype=dtype, count=count).reshape(shape)
     return arr
 
 
