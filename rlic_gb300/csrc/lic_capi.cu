@@ -564,9 +564,13 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
         // group's first ones (launches on one stream would each drain first)
         second = chunked ? aux_stream(&e, false) : nullptr;
         if (chunked && !second) return cuda_fail(e, "cudaStreamCreate");
-        // the packs OR into the field's NaN flag; the traced pass reads it
+        // the packs OR into the field's NaN flag, which the traced pass reads,
+        // and the texture's uploads (or its check) into d_flag, which follows
+        // it in the scratch: one memset clears both
         unsigned* nan_flag = reinterpret_cast<unsigned*>(ws + wl.nan);
-        RLIC_CUDA_TRY(cudaMemsetAsync(nan_flag, 0, sizeof(unsigned), stream));
+        RLIC_CUDA_TRY(
+            cudaMemsetAsync(nan_flag, 0, (wl.total - wl.nan) + sizeof(unsigned), stream));
+        const bool check = (flags & RLIC_FLAG_CHECK_TEXTURE) != 0;
         // the scratch was allocated stream-ordered on `stream`
         if (chunked) {
             RLIC_CUDA_TRY(cudaEventRecord(events[nchunks], stream));
@@ -614,7 +618,8 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
                 void* uv_rows = uvb + off * 2 * sizeof(T);
                 if (strided || direct) {  // kernels reading the caller's memory: no host stall
                     RLIC_CUDA_TRY(rlic::launch_gather_strided(texture + r0 * st[0], st[0], st[1],
-                                                              d_tex + off, r1 - r0, nx, aux));
+                                                              d_tex + off, r1 - r0, nx, aux,
+                                                              check ? d_flag : nullptr));
                     RLIC_CUDA_TRY(rlic::launch_pack_strided(u + r0 * st[2], st[2], st[3],
                                                             v + r0 * st[4], st[4], st[5],
                                                             uv_rows, r1 - r0, nx, aux, nan_flag));
@@ -659,7 +664,8 @@ int convolve_impl(const T* texture, const T* u, const T* v, int64_t ny, int64_t 
             RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks + 1], 0));
             RLIC_CUDA_TRY(cudaStreamWaitEvent(stream, events[nchunks - 1], 0));
         }
-        if (flags & RLIC_FLAG_CHECK_TEXTURE)
+        // copied uploads: the texture's check is a pass of its own
+        if (check && !(strided || direct))
             RLIC_CUDA_TRY(rlic::launch_check_negative(d_tex, int64_t(n), d_flag, stream));
         const T* src = dst_of(0);
         // every chunk has arrived: the field's NaN flag is final

@@ -587,11 +587,16 @@ lic_kernel_grad_kernel(const T* __restrict__ g, const T* __restrict__ x,
 #endif
 constexpr int kUploadUnroll = 8;
 
-// dst[i * nx + j] = src[i * s0 + j * s1]
+// dst[i * nx + j] = src[i * s0 + j * s1]; with neg_flag, also sets *neg_flag
+// when an element is below zero (NaN and -0.0 are not: the test of numpy's
+// `np.any(texture < 0)`, src/rlic/_lib.py:174), so the texture's check needs
+// no pass of its own.
 template <typename T>
 __global__ void gather_strided_kernel(const T* __restrict__ src, int64_t s0, int64_t s1,
-                                      T* __restrict__ dst, int64_t ny, int64_t nx) {
+                                      T* __restrict__ dst, int64_t ny, int64_t nx,
+                                      unsigned* __restrict__ neg_flag) {
     const int64_t span = int64_t(blockDim.x) * kUploadUnroll;
+    bool neg = false;
     for (int64_t i = blockIdx.y; i < ny; i += gridDim.y) {
         for (int64_t j0 = int64_t(blockIdx.x) * span + threadIdx.x; j0 < nx;
              j0 += int64_t(gridDim.x) * span) {
@@ -604,10 +609,14 @@ __global__ void gather_strided_kernel(const T* __restrict__ src, int64_t s0, int
 #pragma unroll
             for (int k = 0; k < kUploadUnroll; ++k) {
                 const int64_t j = j0 + int64_t(k) * blockDim.x;
-                if (j < nx) dst[i * nx + j] = r[k];
+                if (j < nx) {
+                    neg |= r[k] < T(0);
+                    dst[i * nx + j] = r[k];
+                }
             }
         }
     }
+    if (neg && neg_flag) atomicOr(neg_flag, 1u);
 }
 
 // uv[i * nx + j] = (u[i * su0 + j * su1], v[i * sv0 + j * sv1])
@@ -644,12 +653,27 @@ __global__ void pack_uv_strided_kernel(const T* __restrict__ u, int64_t su0, int
     if (nan && nan_flag) atomicOr(nan_flag, 1u);
 }
 
-// Contiguous rows with 16-byte aligned starts: plain 16-byte vector copies
-// (T only tags the instantiation of each translation unit).
+// Whether an element of a 16-byte vector of T is below zero (NaN and -0.0
+// are not).
+template <typename T>
+__device__ __forceinline__ bool negative_in(uint4 w) {
+    if constexpr (sizeof(T) == 4) {
+        return (__uint_as_float(w.x) < 0.f) | (__uint_as_float(w.y) < 0.f) |
+               (__uint_as_float(w.z) < 0.f) | (__uint_as_float(w.w) < 0.f);
+    } else {
+        const double a = __longlong_as_double(static_cast<long long>(uint64_t(w.y) << 32 | w.x));
+        const double b = __longlong_as_double(static_cast<long long>(uint64_t(w.w) << 32 | w.z));
+        return (a < 0.0) | (b < 0.0);
+    }
+}
+
+// Contiguous rows with 16-byte aligned starts: plain 16-byte vector copies of
+// elements of type T; with neg_flag, as gather_strided_kernel.
 template <typename T>
 __global__ void copy_vec16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
-                                  int64_t nvec) {
+                                  int64_t nvec, unsigned* __restrict__ neg_flag) {
     const int64_t span = int64_t(blockDim.x) * kUploadUnroll;
+    bool neg = false;
     for (int64_t b = int64_t(blockIdx.x) * span + threadIdx.x; b < nvec;
          b += int64_t(gridDim.x) * span) {
         uint4 r[kUploadUnroll];
@@ -661,9 +685,13 @@ __global__ void copy_vec16_kernel(const uint4* __restrict__ src, uint4* __restri
 #pragma unroll
         for (int k = 0; k < kUploadUnroll; ++k) {
             const int64_t q = b + int64_t(k) * blockDim.x;
-            if (q < nvec) dst[q] = r[k];
+            if (q < nvec) {
+                neg |= negative_in<T>(r[k]);
+                dst[q] = r[k];
+            }
         }
     }
+    if (neg && neg_flag) atomicOr(neg_flag, 1u);
 }
 
 // Contiguous u, v with 16-byte aligned rows: 16-byte vectors of u and of v
@@ -1085,16 +1113,16 @@ cudaError_t launch_pack_strided_t(const T* u, int64_t su0, int64_t su1, const T*
 // Rows [0, ny) of a strided array into a contiguous one.
 template <typename T>
 cudaError_t launch_gather_strided_t(const T* src, int64_t s0, int64_t s1, T* dst, int64_t ny,
-                                    int64_t nx, cudaStream_t stream) {
+                                    int64_t nx, cudaStream_t stream, unsigned* neg_flag) {
     const int64_t per_vec = 16 / int64_t(sizeof(T));
     if (s1 == 1 && s0 == nx && nx % per_vec == 0 && aligned16(src) && aligned16(dst)) {
         const int64_t nvec = ny * nx / per_vec;
         const dim3 grid = upload_grid(1, nvec, kUploadUnroll);
-        copy_vec16_kernel<T><<<grid.x, 256, 0, stream>>>(reinterpret_cast<const uint4*>(src),
-                                                         reinterpret_cast<uint4*>(dst), nvec);
+        copy_vec16_kernel<T><<<grid.x, 256, 0, stream>>>(
+            reinterpret_cast<const uint4*>(src), reinterpret_cast<uint4*>(dst), nvec, neg_flag);
     } else {
         gather_strided_kernel<T><<<upload_grid(ny, nx, kUploadUnroll), 256, 0, stream>>>(
-            src, s0, s1, dst, ny, nx);
+            src, s0, s1, dst, ny, nx, neg_flag);
     }
     count_launch();
     return cudaGetLastError();
@@ -1102,8 +1130,6 @@ cudaError_t launch_gather_strided_t(const T* src, int64_t s0, int64_t s1, T* dst
 
 template <typename T>
 cudaError_t launch_check_negative_t(const T* x, int64_t n, unsigned* flag, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(unsigned), stream);
-    if (e != cudaSuccess) return e;
     // whole warps only: every lane of a launched warp reaches the vote
     check_negative_kernel<T><<<stream_blocks(n), 256, 0, stream>>>(x, n, flag);
     count_launch();
@@ -1235,8 +1261,9 @@ cudaError_t launch_kernel_grad_t(const T* g, const T* x, const uint32_t* codes, 
                                         nan_flag);                                           \
     }                                                                                        \
     cudaError_t launch_gather_strided(const T* src, int64_t s0, int64_t s1, T* dst,          \
-                                      int64_t ny, int64_t nx, cudaStream_t stream) {         \
-        return launch_gather_strided_t<T>(src, s0, s1, dst, ny, nx, stream);                 \
+                                      int64_t ny, int64_t nx, cudaStream_t stream,           \
+                                      unsigned* neg_flag) {                                  \
+        return launch_gather_strided_t<T>(src, s0, s1, dst, ny, nx, stream, neg_flag);       \
     }                                                                                        \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel, int klen, \
                                const Shape& sh, T* y, cudaStream_t stream) {                 \

@@ -109,13 +109,14 @@ inline bool paired_launch_fits(int64_t npix, int block_x, int block_y, int64_t k
     cudaError_t launch_from_storage(const void* src, int storage, const double* undo,      \
                                     T* dst, int64_t n, cudaStream_t stream);               \
     cudaError_t launch_check_negative(const T* x, int64_t n, unsigned* flag,               \
-                                      cudaStream_t stream);                                \
+                                      cudaStream_t stream); /* flag zeroed by the caller */ \
     cudaError_t launch_pack_strided(const T* u, int64_t su0, int64_t su1, const T* v,      \
                                     int64_t sv0, int64_t sv1, void* uv, int64_t ny,        \
                                     int64_t nx, cudaStream_t stream,                       \
                                     unsigned* nan_flag = nullptr);                         \
     cudaError_t launch_gather_strided(const T* src, int64_t s0, int64_t s1, T* dst,        \
-                                      int64_t ny, int64_t nx, cudaStream_t stream);        \
+                                      int64_t ny, int64_t nx, cudaStream_t stream,         \
+                                      unsigned* neg_flag = nullptr);                       \
     cudaError_t launch_scatter(const T* g, const uint32_t* codes, const T* kernel,         \
                                int klen, const Shape& sh, T* y, cudaStream_t stream);      \
     cudaError_t launch_kernel_grad(const T* g, const T* x, const uint32_t* codes,          \

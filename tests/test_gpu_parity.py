@@ -532,6 +532,46 @@ def test_host_path_checks_negative_texture_on_device() -> None:
     assert [type(e) for e in info.value.exceptions] == [ValueError, ValueError]
 
 
+_NEGATIVE_MSG = r"^Found invalid texture element\(s\)\. Expected only positive values\.$"
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("layout", ["contiguous", "transposed", "odd_width", "chunked"])
+def test_texture_check_in_every_upload_form(dtype, layout) -> None:
+    """The texture's scan for elements below zero runs inside its upload, in
+    each upload form: 16-byte vector copies (contiguous rows), element
+    gathers (a transposed view, rows of a width that is no multiple of 16
+    bytes) and row chunks (4 Mpx), with the element in the last rows read.
+    -0.0, NaN and +inf are not below zero; -inf and the smallest subnormal
+    below zero are."""
+    ny, nx = {"contiguous": (96, 128), "transposed": (96, 128), "odd_width": (90, 127),
+              "chunked": (2048, 2048)}[layout]
+    rng = np.random.default_rng(47)
+    tex = rng.random((ny, nx)).astype(dtype)
+    u, v = _field(rng, ny, nx, dtype, "random")
+    k = np.hanning(9).astype(dtype)
+
+    def shaped(a: np.ndarray) -> np.ndarray:
+        return np.ascontiguousarray(a.T).T if layout == "transposed" else a
+
+    tiny = np.finfo(dtype).smallest_subnormal
+    for value in (-1.0, -np.inf, -tiny):
+        bad = tex.copy()
+        bad[ny - 1, nx - 2] = value
+        with pytest.raises(ValueError, match=_NEGATIVE_MSG):
+            rlic_gb300.convolve(shaped(bad), shaped(u), shaped(v), kernel=k, iterations=2)
+    ok = tex.copy()
+    ok[ny - 1, nx - 1] = -0.0
+    ok[ny - 1, nx - 2] = np.nan
+    ok[ny - 1, nx - 3] = np.inf
+    got = rlic_gb300.convolve(shaped(ok), shaped(u), shaped(v), kernel=k, iterations=2)
+    assert got.shape == (ny, nx)
+    # the scan leaves the convolution itself alone
+    want = rlic_gb300.convolve(tex, u, v, kernel=k, iterations=2)
+    assert_bitwise(rlic_gb300.convolve(shaped(tex), shaped(u), shaped(v), kernel=k,
+                                       iterations=2), want)
+
+
 def test_host_path_without_direct_access(tmp_path) -> None:
     """The copy-based host path (devices without pageable-memory access) gives
     the same bits as the direct one."""
@@ -552,6 +592,17 @@ def test_host_path_without_direct_access(tmp_path) -> None:
         "out = rlic_gb300.convolve(c['texture'], c['u'], c['v'], kernel=c['kernel'],\n"
         "                          boundaries='periodic', iterations=2)\n"
         f"np.save({str(tmp_path / 'big.npy')!r}, out)\n"
+        # copied uploads scan the texture in a pass of their own
+        "for n in (96, 2100):\n"
+        "    c = readme_case(n=n)\n"
+        "    c['texture'][n - 1, 3] = -1.0\n"
+        "    try:\n"
+        "        rlic_gb300.convolve(c['texture'], c['u'], c['v'], kernel=c['kernel'],\n"
+        "                            iterations=2)\n"
+        "    except ValueError as exc:\n"
+        "        assert str(exc).startswith('Found invalid texture'), exc\n"
+        "    else:\n"
+        "        raise SystemExit('a negative texture element was not reported')\n"
     )
     env = dict(__import__("os").environ, RLIC_NO_HOST_DIRECT="1")
     subprocess.run([sys.executable, str(script)], check=True, env=env, timeout=300)
