@@ -408,10 +408,11 @@ def test_launches_are_counted() -> None:
     before = _native.launch_count()
     c = readme_case(n=64)
     u, v = np.ascontiguousarray(c["u"]), np.ascontiguousarray(c["v"])
-    # texture check + pack + traced pass + 2 replays, plus the texture upload
-    # as a gather kernel where the device reads host memory in place (else a
-    # copy-engine copy); one row chunk at this size
-    want = 6 if _native.lib().rlic_host_direct_access() else 5
+    # pack + traced pass + 2 replays, plus the texture upload as a gather
+    # kernel that also scans it for negative elements where the device reads
+    # host memory in place (else a copy-engine copy and a scan kernel); one
+    # row chunk at this size
+    want = 5
     rlic_gb300.convolve(c["texture"], u, v, kernel=c["kernel"], iterations=3)
     assert _native.launch_count() - before == want
     before = _native.launch_count()
