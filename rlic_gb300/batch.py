@@ -55,6 +55,8 @@ def _validate_item(k: int, item: dict) -> tuple:
         item.get("boundaries", "closed"), item.get("iterations", 1),
     )
     if len(problems) == 1:
+        # convolve's message, with the item's index as a note
+        problems[0].add_note(f"in batch item {k}")
         raise problems[0]
     if problems:
         raise ExceptionGroup(f"Invalid inputs were received (batch item {k}).", problems)
