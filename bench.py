@@ -660,7 +660,7 @@ def run_readme(args) -> None:
         rlic_gb300.convolve(c["texture"], c["u"], c["v"], kernel=c["kernel"], boundaries="periodic")
     e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
     res = {}
-    for threads in (1, oracle.env_threads()):
+    for threads in () if args.no_cpu_baseline else (1, oracle.env_threads()):
         t0 = time.perf_counter()
         reps = 3
         for _ in range(reps):
