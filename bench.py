@@ -28,7 +28,10 @@ built here), with the same metric and config.
 
 Multi-GPU (torchrun, one rank per GPU): every rank convolves its own full
 instance (the image does not need to be split to fill a GPU), so the work
-per GPU is fixed and value = total samples / max time over ranks.
+per GPU is fixed and value = total samples / max time over ranks.  With
+--shard one image is split into row bands instead, and with --workload
+batched the 64-instance batch is split by instance; both are strong
+scaling (the work is fixed).
 """
 
 from __future__ import annotations
@@ -907,6 +910,61 @@ def run_batched(args) -> None:
     }), flush=True)
 
 
+def run_batched_sharded(args, dist: Dist) -> None:
+    """The 64-instance batch (seed 3) split by instance across the ranks
+    (rlic_gb300.batch.shard_items: whole instances, balanced by samples, no
+    data exchanged).  Each rank tunes and records its share as a CUDA graph
+    and replays it; value = the whole batch's samples per second over the
+    slowest rank (strong scaling: the batch is fixed)."""
+    import torch
+
+    from rlic_gb300.batch import BatchPlan, autotune_tiles, item_samples, shard_items
+    from rlic_gb300.workloads import batch_case
+
+    dist.init("nccl")
+    dev = torch.device("cuda", dist.local_rank)
+    torch.cuda.set_device(dev)
+    items = batch_case(count=64, seed=3, device="cpu")
+    total = sum(item_samples(it) for it in items)
+    mine = shard_items(items, dist.world)[dist.rank]
+    share = [{**items[k], **{x: items[k][x].to(dev) for x in ("texture", "u", "v", "kernel")}}
+             for k in mine]
+    plan = None
+    if share:
+        autotune_tiles(share)
+        plan = BatchPlan(share)
+        plan.capture()
+    stream = torch.cuda.current_stream(dev)
+    steps = max(3, min(args.steps, 10))
+    for _ in range(max(3, args.warmup)):
+        if plan is not None:
+            plan.replay()
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    ev0.record(stream)
+    for _ in range(steps):
+        if plan is not None:
+            plan.replay()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    ms = dist.max(ev0.elapsed_time(ev1), dev) / steps
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": total / (ms / 1e3) / 1e9, "unit": UNIT,
+            "n_gpus": dist.world, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (batch_case: 64 instances, seed 3)",
+            "workload": "batch_64_instances_seed3",
+            "config": {"workload": "batch_64_instances_seed3", "instances": len(items),
+                       "sharding": f"{dist.world} ranks, whole instances balanced by samples, "
+                                   "no exchange"},
+        }), flush=True)
+    dist.close()
+
+
 def run_shard(args, dist: Dist) -> None:
     """Strong scaling of one image: the 8192^2 workload split into row bands,
     one per rank (rlic_gb300.sharding), each band device-resident with its
@@ -983,7 +1041,10 @@ def main() -> None:
     elif args.workload == "equalize":
         run_equalize(args)
     elif args.workload == "batched":
-        run_batched(args)
+        if dist.world > 1:
+            run_batched_sharded(args, dist)
+        else:
+            run_batched(args)
     elif args.shard:
         run_shard(args, dist)
     else:

@@ -25,11 +25,17 @@ uv mode), the CTA tile shape (``tile_x`` x 256 / ``tile_x`` pixels) and the
 tiles per replay work item (``replay_tiles``) by timing the candidates on
 the bucket's first item.  Results are bit-identical to one ``convolve`` call
 per item, whatever the tile shapes.
+
+On several GPUs a batch shards by instance: ``shard_items`` gives each rank
+whole items, balanced by samples, and ``convolve_batch_sharded`` runs one
+rank's share; the instances are independent, so no data moves between
+ranks.
 """
 
 from __future__ import annotations
 
-__all__ = ["BatchPlan", "autotune_tiles", "convolve_batch"]
+__all__ = ["BatchPlan", "autotune_tiles", "convolve_batch", "convolve_batch_sharded",
+           "item_samples", "shard_items"]
 
 import ctypes
 import math
@@ -178,6 +184,48 @@ class BatchPlan:
 def convolve_batch(items: list[dict]) -> list:
     """One-shot batch: validate, run, and return the outputs."""
     return BatchPlan(items).run()
+
+
+def item_samples(item: dict) -> int:
+    """Samples of one item: pixels x kernel length x iterations."""
+    ny, nx = item["texture"].shape
+    return int(ny) * int(nx) * int(item["kernel"].shape[0]) * int(item.get("iterations", 1))
+
+
+def shard_items(items: list[dict], world: int) -> list[list[int]]:
+    """The item indices each of `world` ranks runs, for one batch on several
+    GPUs.
+
+    Instances are independent, so each goes whole to one rank and no data
+    moves between ranks.  Largest first (by samples), each item goes to the
+    rank with the fewest samples so far (the lowest rank on a tie), so that
+    the ranks' totals differ by at most the samples of one item (Graham's
+    longest-processing-time rule).  The assignment depends on the items
+    alone: every rank computes the same one without a message.
+    """
+    if world <= 0:
+        raise ValueError("world size must be positive")
+    load = [0] * world
+    shares: list[list[int]] = [[] for _ in range(world)]
+    for k in sorted(range(len(items)), key=lambda k: (-item_samples(items[k]), k)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        shares[r].append(k)
+        load[r] += item_samples(items[k])
+    return [sorted(s) for s in shares]
+
+
+def convolve_batch_sharded(items: list[dict], rank: int, world: int, run=None) -> dict:
+    """This rank's share of a batch run on `world` ranks (``shard_items``):
+    {item index: output}.  ``run`` maps a list of items to their outputs
+    (default ``convolve_batch``, on this rank's GPU); the union over ranks
+    holds every item's output once."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside a world of {world}")
+    mine = shard_items(items, world)[rank]
+    if not mine:
+        return {}
+    outs = (run or convolve_batch)([items[k] for k in mine])
+    return dict(zip(mine, outs))
 
 
 def _bucket(item: dict) -> tuple:

@@ -8,6 +8,8 @@ are refused, naming the item at fault.
 
 from __future__ import annotations
 
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -68,3 +70,113 @@ def test_mismatched_dtypes_raise_convolves_type_error() -> None:
     item["u"] = item["u"].double()
     with pytest.raises(TypeError, match="Data types mismatch"):
         BatchPlan([item])
+
+
+# ------------------------------------------------------- instance sharding --
+
+def _sized_items(sides_klens_iters) -> list[dict]:
+    items = []
+    for ny, nx, klen, n in sides_klens_iters:
+        items.append({"texture": np.zeros((ny, nx)), "u": None, "v": None,
+                      "kernel": np.zeros(klen), "iterations": n})
+    return items
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 5, 8])
+def test_shard_items_is_a_balanced_partition(world) -> None:
+    from rlic_gb300.batch import item_samples, shard_items
+
+    rng = np.random.default_rng(world)
+    items = _sized_items(
+        (int(rng.integers(8, 300)), int(rng.integers(8, 300)), int(rng.integers(1, 65)) * 2 + 1,
+         int(rng.integers(1, 11))) for _ in range(37))
+    shares = shard_items(items, world)
+    assert len(shares) == world
+    flat = sorted(k for s in shares for k in s)
+    assert flat == list(range(len(items)))
+    assert all(s == sorted(s) for s in shares)
+    loads = [sum(item_samples(items[k]) for k in s) for s in shares]
+    assert max(loads) - min(loads) <= max(item_samples(i) for i in items)
+    # the same items give the same assignment on every rank
+    assert shard_items(items, world) == shares
+
+
+def test_shard_items_edge_cases() -> None:
+    from rlic_gb300.batch import convolve_batch_sharded, shard_items
+
+    items = _sized_items([(4, 4, 3, 1), (64, 64, 9, 2), (8, 8, 5, 1)])
+    # more ranks than items: the largest items first, each to an idle rank
+    assert shard_items(items, 5) == [[1], [2], [0], [], []]
+    assert shard_items([], 3) == [[], [], []]
+    assert shard_items(items, 1) == [[0, 1, 2]]
+    with pytest.raises(ValueError, match="world size"):
+        shard_items(items, 0)
+    with pytest.raises(ValueError, match="outside a world"):
+        convolve_batch_sharded(items, 2, 2)
+    # an idle rank runs nothing
+    assert convolve_batch_sharded(items, 4, 5, run=lambda its: 1 / 0) == {}
+
+
+def _oracle_item(oracle, it: dict) -> np.ndarray:
+    return oracle.convolve(it["texture"].numpy(), it["u"].numpy(), it["v"].numpy(),
+                           it["kernel"].numpy(), uv_mode=it["uv_mode"],
+                           boundaries=it["boundaries"], iterations=it["iterations"])
+
+
+def _batch_worker(rank, world, port, outdir, seed) -> None:
+    import os
+
+    import torch.distributed as dist
+
+    from oracle import oracle
+    from rlic_gb300.batch import convolve_batch_sharded
+    from rlic_gb300.workloads import batch_case
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        items = batch_case(count=9, seed=seed, min_side=16, max_side=48, device="cpu")
+
+        def run(share):
+            return [_oracle_item(oracle, it) for it in share]
+
+        mine = convolve_batch_sharded(items, rank, world, run=run)
+        # the ranks' shares partition the batch without any exchange before
+        # this check
+        every = [None] * world
+        dist.all_gather_object(every, sorted(mine))
+        assert sorted(k for s in every for k in s) == list(range(len(items)))
+        np.savez(Path(outdir) / f"rank{rank}.npz",
+                 **{f"item{k}": out for k, out in mine.items()})
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_batch_on_gloo_ranks(tmp_path, oracle, world) -> None:
+    """A batch sharded by instance over gloo ranks (the oracle standing in
+    for each rank's GPU): every item's output exactly once, equal to the
+    item run alone."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    from rlic_gb300.workloads import batch_case
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    seed = 11
+    mp.spawn(_batch_worker, nprocs=world, join=True, args=(world, port, str(tmp_path), seed))
+    items = batch_case(count=9, seed=seed, min_side=16, max_side=48, device="cpu")
+    got = {}
+    for r in range(world):
+        with np.load(tmp_path / f"rank{r}.npz") as z:
+            for name in z.files:
+                k = int(name[4:])
+                assert k not in got
+                got[k] = z[name]
+    assert sorted(got) == list(range(len(items)))
+    for k, it in enumerate(items):
+        np.testing.assert_array_equal(got[k], _oracle_item(oracle, it))
