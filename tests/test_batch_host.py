@@ -180,3 +180,45 @@ def test_sharded_batch_on_gloo_ranks(tmp_path, oracle, world) -> None:
     assert sorted(got) == list(range(len(items)))
     for k, it in enumerate(items):
         np.testing.assert_array_equal(got[k], _oracle_item(oracle, it))
+
+
+def test_autotune_times_one_item_per_bucket(monkeypatch) -> None:
+    """The tuner's choices, with the timing replaced by a fixed cost table:
+    one probe per bucket (side, kernel length in steps of 32 taps, uv mode),
+    probes of at most two iterations, the fastest tile shape, then the
+    fastest tiles per replay item with it, and no replay choice for
+    single-pass probes."""
+    from rlic_gb300 import batch
+
+    probes = []
+
+    class FakePlan:
+        def __init__(self, items, queue=False, solo_pixels=batch.SOLO_PIXELS) -> None:
+            assert len(items) == 1 and solo_pixels == 0
+            self.item, self.queue = items[0], queue
+
+    def fake_time(plan, repeats) -> float:
+        it = plan.item
+        probes.append((it["texture"].shape, it["iterations"], it["tile_x"],
+                       it.get("replay_tiles"), plan.queue))
+        cost = {64: 3.0, 32: 1.0, 16: 2.0}[it["tile_x"]]
+        if plan.queue:
+            cost += {2: 2.0, 4: 1.0, 8: 3.0}[it["replay_tiles"]]
+        return cost
+
+    monkeypatch.setattr(batch, "BatchPlan", FakePlan)
+    monkeypatch.setattr(batch, "_time_plan", fake_time)
+    items = _sized_items([(256, 256, 65, 5), (256, 256, 63, 9), (64, 64, 9, 1),
+                          (256, 256, 65, 3)])
+    for it in items:
+        it["uv_mode"] = "velocity"
+    items[3]["uv_mode"] = "polarization"
+    choice = batch.autotune_tiles(items)
+    # buckets: items 0 and 1 share one (same side, 33-64 taps, velocity)
+    assert len(choice) == 3
+    assert [(it["tile_x"], it["replay_tiles"]) for it in items] == [
+        (32, 4), (32, 4), (32, 0), (32, 4)]
+    # 3 tile shapes per bucket, plus 3 replay choices where the probe has a replay
+    assert len(probes) == 3 * 3 + 2 * 3
+    assert all(n <= 2 for _, n, _, _, _ in probes)
+    assert not any(q for shape, _, _, _, q in probes if shape == (64, 64))
