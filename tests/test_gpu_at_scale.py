@@ -22,8 +22,6 @@ workload's exact path); the 64-instance batched mix; 1024^2 float32,
 
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 import pytest
 

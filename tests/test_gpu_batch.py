@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import rlic_gb300
-from rlic_gb300.batch import BatchPlan, autotune_tiles, convolve_batch
+from rlic_gb300.batch import BatchPlan, autotune_tiles
 from rlic_gb300.workloads import batch_case
 
 pytestmark = pytest.mark.gpu
